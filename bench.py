@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark of the batched partitioned-convolution path.
+
+Workload (one "step"): 32 independent mono float32 streams, each 2^19
+samples of N(0, 0.1^2) input followed by zeros to flush its IR (IR lengths
+log-uniform in [2^14, 2^19] taps, T60 U(0.3, 4) s, seeded), base block 256,
+layouts from the minimum-slack level chain, all streams in one handle: every
+256-sample base block is one launch per kernel class, replayed from CUDA
+graphs.  A step starts from reset state and processes the whole workload.
+
+Metric: audio-seconds processed per second (48 kHz).  ``value`` runs on
+device-resident inputs; ``e2e`` goes through the C ABI (pc_process) with
+pinned host buffers, host<->device copies inside the timed region.  The
+per-stream drop-in path (one handle and one pc_run call per stream per
+block) is timed on a bounded sample as ``plain_gpu``.  ``cpu_baseline`` is
+the oracle restatement of the reference CPU path on all host cores.
+
+--impl reference times that CPU restatement alone (the reference's FFTW
+build cannot be compiled here) on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FS = 48000
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--streams", type=int, default=32)
+    ap.add_argument("--samples", type=int, default=1 << 19)
+    ap.add_argument("--plain-blocks", type=int, default=96, help="pc_run calls per stream in the plain sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0, help="base steps for the per-kernel profile (0: 4*H)")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.idx)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.strip().split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = max(smax, float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# --------------------------------------------------------------------------
+def workload(streams: int, samples: int):
+    from partconv_gb300 import workloads as wl
+
+    c = wl.cfg2(n_streams=streams, n_samples=samples)
+    N0 = c["N0"]
+    tail = max(len(h) for h in c["irs"])
+    frames = samples + (tail + N0 - 1) // N0 * N0
+    x = np.zeros((streams, frames), np.float32)
+    x[:, :samples] = c["x"]
+    return c, x, frames
+
+
+def bytes_per_sample(layouts):
+    from partconv_gb300 import workloads as wl
+
+    return float(np.mean([wl.algorithmic_bytes_per_sample(N, P) for N, P in layouts]))
+
+
+def cpu_baseline(c, x, frames, max_seconds=20.0, threads=None):
+    """Oracle restatement on host threads over a bounded prefix of every
+    stream; returns (audio-s/s, cores, sample description, elapsed)."""
+    import oracle
+
+    threads = threads or os.cpu_count() or 1
+    S = x.shape[0]
+    N0 = c["N0"]
+    # probe 1/16 of the workload, then size the sample to ~max_seconds
+    probe = max(N0 * 64, (frames // 16) // N0 * N0)
+    _, t = oracle.run_streams(c["layouts"], c["irs"], x[:, :probe], N0, threads)
+    rate = S * probe / max(t, 1e-9)
+    n = int(min(frames, max(probe, rate * max_seconds / S)) // N0 * N0)
+    _, t = oracle.run_streams(c["layouts"], c["irs"], x[:, :n], N0, threads)
+    return S * n / FS / t, threads, f"first {n} of {frames} samples of all {S} streams", t
+
+
+# --------------------------------------------------------------------------
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    c, x, frames = workload(args.streams, args.samples)
+    import oracle
+
+    threads = os.cpu_count() or 1
+    N0 = c["N0"]
+    S = x.shape[0]
+    # bounded sample per step: sized from a probe to ~8 s per step
+    probe = (frames // 32) // N0 * N0
+    _, t = oracle.run_streams(c["layouts"], c["irs"], x[:, :probe], N0, threads)
+    n = int(min(frames, max(probe, probe * 8.0 / max(t, 1e-9))) // N0 * N0)
+    for _ in range(args.warmup):
+        oracle.run_streams(c["layouts"], c["irs"], x[:, :n], N0, threads)
+    times = []
+    for _ in range(args.steps):
+        _, t = oracle.run_streams(c["layouts"], c["irs"], x[:, :n], N0, threads)
+        times.append(t)
+    sec = float(np.mean(times))
+    v = S * n / FS / sec
+    sample = f"first {n} of {frames} samples of all {S} streams per step"
+    line = {
+        "impl": "reference", "metric": "audio-s/s (batched partitioned convolution, 32 streams, N0=256)",
+        "value": v, "unit": "audio-s/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "cfg2: 32 streams x 2^19 samples, IR 2^14..2^19 taps, N0=256", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "audio-s/s", "cores": threads, "kind": "port",
+                         "sample": sample + "; restated CPU path (own FFT); reference FFTW build unavailable"},
+        "e2e": {"value": v, "unit": "audio-s/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    from partconv_gb300 import PC_PLANAR, PartConvMulti
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    c, x_host, frames = workload(args.streams, args.samples)
+    S, N0 = x_host.shape[0], c["N0"]
+    pcs = [dict(ir=h, N=N, P=P, in_ch=s, out_ch=s) for s, (h, (N, P)) in enumerate(zip(c["irs"], c["layouts"]))]
+    m = PartConvMulti()
+    m.setup_layout(FS, N0, S, S, pcs)
+    info = m.info()
+    audio_s = S * frames / FS
+
+    x = torch.from_numpy(x_host).to(dev)
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)   # 256 MB > L2
+
+    def one_step():
+        m.reset()
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.process_device(y, x, frames, PC_PLANAR, stream)
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+
+    # ---- parity of the benchmarked output (last warm-up) vs the oracle -----
+    parity = None
+    if not args.no_parity and rank == 0:
+        import oracle
+        from partconv_gb300 import workloads as wl
+
+        y_np = y.cpu().numpy()
+        t0 = time.time()
+        ref, t_or = oracle.run_streams(c["layouts"], c["irs"], x_host, N0)
+        errs = [wl.rel_l2(y_np[s], ref[s]) for s in range(S)]
+        parity = {"rel_l2_max_vs_oracle": max(errs), "tol": 1e-5, "oracle_seconds": time.time() - t0}
+
+    # ---- timed region -----------------------------------------------------------
+    clocks = ClockSampler(local)
+    launches0 = m.kernel_launches()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    w0 = time.perf_counter()
+    evs = [one_step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    launches = m.kernel_launches() - launches0
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * audio_s / (ms / 1e3)
+
+    # ---- e2e: host buffers through the C ABI (pinned), copies timed -------------
+    xp = torch.from_numpy(x_host).pin_memory()
+    yp = torch.empty_like(xp).pin_memory()
+    m.reset()
+    m.process_into(yp.data_ptr(), xp.data_ptr(), frames, PC_PLANAR)   # grows device buffers once
+    e2e_times = []
+    for _ in range(max(1, args.steps)):
+        m.reset()
+        t0 = time.perf_counter()
+        m.process_into(yp.data_ptr(), xp.data_ptr(), frames, PC_PLANAR)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_v = ws * audio_s / float(np.mean(e2e_times))
+    nbytes = x_host.nbytes
+
+    # ---- per-kernel profile for the roofline --------------------------------------
+    m.reset()
+    prof_steps = args.profile_steps or max(4 * info.hyperperiod, 256)
+    m.process_device(y, x, frames, PC_PLANAR, stream)   # fill state (steady-state FDL)
+    torch.cuda.synchronize()
+    prof = m.profile_kernels(prof_steps)
+    dom = max(prof, key=lambda r: r["total_ms"])
+    per_launch_s = dom["total_ms"] / 1e3 / dom["launches"]
+    per_launch_b = dom["alg_bytes"] / dom["launches"]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = per_launch_b / per_launch_s / 1e9
+    traffic = ncu_traffic().get(dom["name"])
+    kernels = {r["name"]: {"launches": r["launches"], "avg_us": r["total_ms"] * 1e3 / r["launches"],
+                           "share": r["total_ms"] / sum(q["total_ms"] for q in prof),
+                           "alg_bytes_per_launch": r["alg_bytes"] / r["launches"],
+                           "achieved_gbs": r["alg_bytes"] / (r["total_ms"] / 1e3) / 1e9} for r in prof}
+
+    # ---- plain per-stream drop-in path (bounded sample) -----------------------------
+    plain = None
+    if rank == 0 and args.plain_blocks > 0:
+        hs = []
+        for s in range(S):
+            ms_ = PartConvMulti()
+            ms_.setup_layout(FS, N0, 1, 1, [pcs[s] | dict(in_ch=0, out_ch=0)])
+            hs.append(ms_)
+        buf = np.zeros(N0, np.float32)
+        lat = []
+        R = args.plain_blocks
+        for b in range(8):   # warm
+            for s in range(S):
+                hs[s].run(buf, x_host[s, b * N0:(b + 1) * N0], N0)
+        t0 = time.perf_counter()
+        for b in range(R):
+            for s in range(S):
+                a = time.perf_counter()
+                hs[s].run(buf, x_host[s, b * N0:(b + 1) * N0], N0)
+                lat.append(time.perf_counter() - a)
+        tp = time.perf_counter() - t0
+        plain_v = S * R * N0 / FS / tp
+        plain = {"value": plain_v, "unit": "audio-s/s",
+                 "sample": f"{R} pc_run calls per stream x {S} streams (one handle per stream)",
+                 "pc_run_latency_us": {"p50": float(np.percentile(lat, 50) * 1e6),
+                                       "p99": float(np.percentile(lat, 99) * 1e6)}}
+        del hs
+
+    # ---- batched per-block latency: one base step of all streams, device time ------
+    # (one block of all streams is contiguous in the interleaved layout)
+    m.reset()
+    nlat = min(frames // N0, max(2 * info.hyperperiod, 256))
+    step_ms = []
+    xi = torch.from_numpy(np.ascontiguousarray(x_host[:, : nlat * N0].T)).to(dev)
+    yi = torch.empty_like(xi)
+    for b in range(nlat):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.process_device(yi[b * N0:(b + 1) * N0], xi[b * N0:(b + 1) * N0], N0, 0, stream)
+        e1.record(stream)
+        step_ms.append((e0, e1))
+    torch.cuda.synchronize()
+    lat_us = [a.elapsed_time(b) * 1e3 for a, b in step_ms]
+
+    # ---- CPU baseline (oracle port, all host threads, bounded sample) ------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, sample, _ = cpu_baseline(c, x_host, frames)
+        cpu = {"value": v, "unit": "audio-s/s", "cores": cores, "kind": "port",
+               "sample": sample + "; restated CPU path (own FFT); reference FFTW build unavailable"}
+
+    if rank == 0:
+        bps = bytes_per_sample(c["layouts"])
+        line = {
+            "metric": "audio-s/s (batched partitioned convolution, 32 streams, N0=256)",
+            "value": value, "unit": "audio-s/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded numpy PCG64, cfg seed 1002)",
+            "config": {"workload": f"cfg2: {S} streams x {args.samples} samples + IR flush ({frames} per stream), "
+                                   f"IR 2^14..2^19 taps, N0={N0}, one handle, graph-replayed base steps",
+                       "layouts": "minimum-slack level chain (ratio 8, max block 16384)",
+                       "streams": S, "frames_per_stream": frames, "N0": N0,
+                       "hyperperiod_steps": info.hyperperiod,
+                       "l2": "256 MB buffer written between timed steps (outside the events); "
+                             "FDL state (%.0f MB) stays L2-resident within a step" % (info.device_bytes / 1e6),
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": e2e_v, "unit": "audio-s/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "how": "pc_process on pinned host buffers (planar), copies inside the timed region"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "alg_bytes_per_launch": per_launch_b, "avg_launch_us": per_launch_s * 1e6},
+            "kernels": kernels,
+            "path_alg_bytes_per_sample": bps,
+            "path_roofline_frac": (bps * S * frames / (ms / 1e3)) / 1e9 / peak,
+            "block_latency_us": {"p50": float(np.percentile(lat_us, 50)), "p99": float(np.percentile(lat_us, 99)),
+                                 "max": float(np.max(lat_us)), "deadline_us": N0 / FS * 1e6,
+                                 "how": "device time of one base step (all streams), single launches"},
+            "wall_s_timed_region": wall,
+        }
+        if plain:
+            line["plain_gpu"] = plain
+            line["batched_over_plain"] = value / plain["value"]
+        if cpu:
+            line["cpu_baseline"] = cpu
+        if parity:
+            line["parity"] = parity
+        if clk:
+            line["clocks"] = clk
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,192 @@
+/*
+ * partconv_gb300.h -- C ABI of the GB300 (sm_103a) partitioned-convolution
+ * engine.
+ *
+ * The engine is a drop-in for PartConvMulti / PartConvMultiRelaxed
+ * (src/partconvMulti.h:52-148 in ebattenberg/partconv).  One handle holds one
+ * multi-instance convolver: a set of partitioned convolvers ("PCs"), each
+ * mapping one input channel through one impulse response (IR) to one output
+ * channel, like a pc.config line.
+ *
+ * Conventions:
+ *   - Every call returns PC_OK (0) or a positive PC_ERR_* code.  Unlike the
+ *     reference, which calls exit(-1) on bad configs and frame counts
+ *     (src/partconvMulti.cpp:31-40, :74-106, :817-821), no call exits the
+ *     process.  pc_last_error() gives the message of the last failure.
+ *   - Host buffers are interleaved float32 [frame][channel] like the
+ *     reference's run() buffers unless a call takes a layout flag.
+ *   - Calls on one handle are not re-entrant (run() in the reference is
+ *     called from one audio thread).  Different handles are independent.
+ *   - Signatures use plain pointers and sizes only; cudaStream_t is passed
+ *     as void*.
+ */
+#ifndef PARTCONV_GB300_H
+#define PARTCONV_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PC_OK 0
+#define PC_ERR_ARG 1      /* bad argument (null pointer, frame count, channel index) */
+#define PC_ERR_LAYOUT 2   /* partition layout rejected (see pc_check_layout) */
+#define PC_ERR_CONFIG 3   /* config file missing or malformed */
+#define PC_ERR_IO 4       /* impulse-response file missing or unreadable */
+#define PC_ERR_CUDA 5     /* CUDA runtime failure or no device */
+#define PC_ERR_NOMEM 6    /* device allocation failed */
+#define PC_ERR_STATE 7    /* call out of order (run before setup, setup twice) */
+#define PC_ERR_LIMIT 8    /* size beyond a documented limit */
+
+/* Interleaved [frame][channel] and planar [channel][frame] host/device layouts. */
+#define PC_INTERLEAVED 0
+#define PC_PLANAR 1
+
+/* Largest block size a level may use (the FFT length is twice this). */
+#define PC_MAX_BLOCK 16384
+/* Most levels one convolver may have. */
+#define PC_MAX_LEVELS 16
+
+typedef struct pc_handle pc_handle;
+
+/* Counters and sizes of a set-up handle (read-only snapshot). */
+typedef struct pc_info {
+    int fs;                  /* sample rate (reported only) */
+    int buffer_size;         /* base block N0 = frames per run() call */
+    int num_input_channels;
+    int num_output_channels;
+    int num_pcs;
+    int max_block_size;
+    int relaxed;             /* 1: PartConvMultiRelaxed semantics */
+    int hyperperiod;         /* steps after which the level schedule repeats */
+    long long frame_num;     /* run() calls so far (PartConvMulti::frameNum) */
+    long long device_bytes;  /* device memory held by the handle */
+} pc_info;
+
+/*
+ * Layout check, host only.  Replaces the validation in
+ * PartConvFilter::setup (src/partconv.cpp:87-181): block sizes are powers of
+ * two and strictly increasing, every level but the last has >= 1 part, the
+ * slack test passes, and the last level is needed.  relaxed = 0 is the
+ * reference's check 2*N0 + s_{L} >= 2*N_{L} (partconv.cpp:148-166);
+ * relaxed = 1 is matlab/MFDL_part_conv.m:25-31, s_L >= N_L.  On success
+ * P[M-1] is recomputed from ir_len (partconv.cpp:169-181) and delays[L]
+ * (may be NULL) gets (2*N0 + s_L)/N0 as in partconv.cpp:148-153.
+ * Also rejects N[M-1] > PC_MAX_BLOCK and M > PC_MAX_LEVELS (PC_ERR_LIMIT).
+ */
+int pc_check_layout(int M, const int* N, int* P, int ir_len, int relaxed, int* delays,
+                    char* msg, int msglen);
+
+/* PartConvMulti(int verbosity) -- src/partconvMulti.h:56. */
+pc_handle* pc_create(int verbosity);
+
+/*
+ * PartConvMulti::setup(config_file, max_threads_per_level, max_level0_threads,
+ * min_work) -- src/partconvMulti.h:58, src/partconvMulti.cpp:23-718.
+ * Parses the pc.config format (header "FS buffer_size nIn nOut numPCs
+ * numRepeats", then per PC "file mute inCh outCh scale M N0 P0 N1 P1 ...",
+ * src/pc.config:43-44) and reads each IR from a WAV file (16/24/32-bit PCM or
+ * 32-bit float, channel 0, like readImpulseResponse in src/sndtools.cpp:3-47).
+ * Relative IR paths are resolved against the config file's directory.
+ * The thread arguments are accepted for signature compatibility; the GPU
+ * schedule has no host worker threads.
+ */
+int pc_setup_config(pc_handle* h, const char* config_file, int max_threads_per_level,
+                    int max_level0_threads, double min_work);
+
+/*
+ * Programmatic setup (no file).  Same semantics as a pc.config with num_pcs
+ * lines: PC i has num_levels[i] levels with block sizes and part counts at
+ * offset sum(num_levels[0..i)) in block_sizes / num_parts (the last level's
+ * part count is ignored and recomputed), IR irs[i] of ir_lens[i] samples,
+ * input channel in_ch[i], output channel out_ch[i], input scale scale[i] and
+ * mute flag mute[i] (muted PCs are computed but not mixed,
+ * partconvMulti.cpp:911-921).  Layouts must pass the relaxed check; every
+ * PC's first block size must equal buffer_size (partconvMulti.cpp:95-101).
+ */
+int pc_setup_layout(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, int num_pcs,
+                    const int* num_levels, const int* block_sizes, const int* num_parts,
+                    const float* const* irs, const int* ir_lens, const int* in_ch,
+                    const int* out_ch, const float* scale, const int* mute);
+
+/*
+ * Selects PartConvMultiRelaxed semantics (src/partconvMulti.h:142-148): the
+ * output of each run() is the previous call's result, one base block later
+ * (src/partconvMulti.cpp:1077-1111).  Call after setup; resets state.
+ */
+int pc_set_relaxed(pc_handle* h, int relaxed);
+
+/*
+ * PartConvMulti::run(output, input, frameCount) -- src/partconvMulti.h:60,
+ * src/partconvMulti.cpp:815-928.  Host interleaved buffers of frame_count ==
+ * buffer_size frames.  Copies the block to the device, runs one base step and
+ * copies the mixed output back before returning.
+ */
+int pc_run(pc_handle* h, float* output, const float* input, int frame_count);
+
+/*
+ * Batched form of run(): frames (a multiple of buffer_size) are processed as
+ * frames/buffer_size consecutive callbacks with results identical to that
+ * many pc_run calls.  Host buffers in the given layout (PC_INTERLEAVED or
+ * PC_PLANAR with row length frames).  Steps run as CUDA-graph replays.
+ * No reference counterpart (the reference has only run()).
+ */
+int pc_process(pc_handle* h, float* output, const float* input, long long frames, int layout);
+
+/*
+ * Same as pc_process with device-resident buffers, enqueued on a caller
+ * stream (void* = cudaStream_t; NULL = the handle's own stream).  Returns
+ * after enqueueing; the caller synchronises the stream.
+ */
+int pc_process_device(pc_handle* h, float* d_output, const float* d_input, long long frames,
+                      int layout, void* stream);
+
+/* PartConvMulti::reset() -- src/partconvMulti.cpp:806-813: clears all state. */
+int pc_reset(pc_handle* h);
+
+/* PartConvMulti::cleanup() -- src/partconvMulti.cpp:720-804: frees device
+ * resources; the handle can be set up again. */
+int pc_cleanup(pc_handle* h);
+
+/* Frees the handle (after cleanup if needed). */
+void pc_destroy(pc_handle* h);
+
+/* Message of the last failing call on h (or of pc_create when h is NULL). */
+const char* pc_last_error(const pc_handle* h);
+
+/* Snapshot of sizes and counters. */
+int pc_get_info(const pc_handle* h, pc_info* info);
+
+/* Partition layout of PC `pc` after setup (last-level part count recomputed). */
+int pc_get_layout(const pc_handle* h, int pc, int* num_levels, int* block_sizes, int* num_parts);
+
+/*
+ * Kernel launches the handle made since creation (every kernel of this
+ * library counts one).  Lets callers check that work ran on the GPU.
+ */
+long long pc_kernel_launches(const pc_handle* h);
+
+/* Per-kernel timing record filled by pc_profile_kernels. */
+typedef struct pc_kernel_stats {
+    char name[32];         /* "fire_small", "fire_mid", "fire_large", "spread_mac" */
+    long long launches;    /* launches that had work in their phase */
+    double total_ms;       /* CUDA-event time summed over those launches */
+    double alg_bytes;      /* algorithmic bytes those launches had to move */
+} pc_kernel_stats;
+
+/*
+ * Profiling aid (no reference counterpart; the reference's
+ * PartConvFilter::bench, src/partconv.cpp:508-566, times one level on the
+ * CPU).  Runs nsteps further base steps from the handle's staging input (the
+ * FDL state continues), launching each kernel separately on the handle's
+ * stream with CUDA events around it, and writes up to max_kinds records.
+ * Algorithmic bytes per level block: filter spectra and input-spectrum rows
+ * read, the new spectrum row written, the 2N-sample window read and N
+ * samples written.
+ */
+int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int max_kinds, int* n_kinds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARTCONV_GB300_H */

@@ -1,0 +1,111 @@
+"""ctypes binding of libpartconv_gb300.so (the C ABI in include/partconv_gb300.h).
+
+Loading never falls back to anything else: if the library is missing or a
+call needs a GPU that is not there, the error propagates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import _build
+
+PC_OK = 0
+PC_ERR_ARG = 1
+PC_ERR_LAYOUT = 2
+PC_ERR_CONFIG = 3
+PC_ERR_IO = 4
+PC_ERR_CUDA = 5
+PC_ERR_NOMEM = 6
+PC_ERR_STATE = 7
+PC_ERR_LIMIT = 8
+PC_INTERLEAVED = 0
+PC_PLANAR = 1
+PC_MAX_BLOCK = 16384
+PC_MAX_LEVELS = 16
+
+_f32p = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int)
+
+
+class PCInfo(C.Structure):
+    _fields_ = [
+        ("fs", C.c_int),
+        ("buffer_size", C.c_int),
+        ("num_input_channels", C.c_int),
+        ("num_output_channels", C.c_int),
+        ("num_pcs", C.c_int),
+        ("max_block_size", C.c_int),
+        ("relaxed", C.c_int),
+        ("hyperperiod", C.c_int),
+        ("frame_num", C.c_longlong),
+        ("device_bytes", C.c_longlong),
+    ]
+
+
+class PCKernelStats(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 32),
+        ("launches", C.c_longlong),
+        ("total_ms", C.c_double),
+        ("alg_bytes", C.c_double),
+    ]
+
+
+# name -> (restype, argtypes); mirrors include/partconv_gb300.h
+SIGNATURES = {
+    "pc_check_layout": (C.c_int, [C.c_int, _i32p, _i32p, C.c_int, C.c_int, _i32p, C.c_char_p, C.c_int]),
+    "pc_create": (C.c_void_p, [C.c_int]),
+    "pc_setup_config": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_double]),
+    "pc_setup_layout": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i32p, _i32p, _i32p,
+                                  C.POINTER(_f32p), _i32p, _i32p, _i32p, _f32p, _i32p]),
+    "pc_set_relaxed": (C.c_int, [C.c_void_p, C.c_int]),
+    "pc_run": (C.c_int, [C.c_void_p, _f32p, _f32p, C.c_int]),
+    "pc_process": (C.c_int, [C.c_void_p, _f32p, _f32p, C.c_longlong, C.c_int]),
+    "pc_process_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "pc_reset": (C.c_int, [C.c_void_p]),
+    "pc_cleanup": (C.c_int, [C.c_void_p]),
+    "pc_destroy": (None, [C.c_void_p]),
+    "pc_last_error": (C.c_char_p, [C.c_void_p]),
+    "pc_get_info": (C.c_int, [C.c_void_p, C.POINTER(PCInfo)]),
+    "pc_get_layout": (C.c_int, [C.c_void_p, C.c_int, _i32p, _i32p, _i32p]),
+    "pc_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "pc_profile_kernels": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(PCKernelStats), C.c_int,
+                                     C.POINTER(C.c_int)]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib(build: bool = True):
+    """Load the in-tree library (building it first when sources changed)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build() if build else _build.LIB_PATH
+            L = C.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+class PartConvError(RuntimeError):
+    """A failing C-ABI call: .code is the PC_ERR_* status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def check(handle, code: int) -> None:
+    if code != PC_OK:
+        msg = lib().pc_last_error(handle)
+        raise PartConvError(code, msg.decode() if msg else "")

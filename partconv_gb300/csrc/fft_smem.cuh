@@ -1,0 +1,155 @@
+// fft_smem.cuh -- shared-memory Stockham FFT and the real-FFT split passes
+// used by the level kernels.
+//
+// A real transform of length 2N (one FDL block window) is computed as the
+// N-point complex FFT of z[n] = x[2n] + i x[2n+1] followed by the split
+// post-pass (X[k] = E[k] + w^k O[k], X[N-k] = conj(E[k] - w^k O[k]),
+// w = e^{-i pi / N}); the inverse runs the matching pre-pass and an
+// unnormalised inverse N-point FFT, giving FFTW c2r's unnormalised output
+// (the 1/nfft factor lives in the filter spectra, as in
+// src/partconv.cpp:216-228 of ebattenberg/partconv).
+//
+// The complex FFT is the Stockham autosort formulation (Govindaraju et al.,
+// "High performance discrete Fourier transforms on graphics processors",
+// SC 2008): radix-4 stages then one radix-2 stage when log2 N is odd.  Each
+// stage stages its butterflies' inputs in registers, so one N-element
+// shared buffer suffices (a barrier separates the reads from the writes).
+//
+// Twiddles come from a table W[m] = exp(-2 pi i m / 2^wlog) computed in
+// double on the host and rounded once to float.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pcg {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+
+// twiddle for a full turn split into 2^lg parts, index m (m < 2^lg)
+__device__ __forceinline__ float2 twiddle(const float2* __restrict__ W, int wlog, int m, int lg, bool inv) {
+    float2 w = __ldg(&W[m << (wlog - lg)]);
+    return inv ? cconj(w) : w;
+}
+
+// One radix-4 Stockham stage (Ns = product of previous radices).
+template <int NT, int MAXB>
+__device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, const float2* __restrict__ W,
+                                         int wlog, bool inv) {
+    const int nb = N >> 2;
+    float2 v[MAXB][4];
+#pragma unroll
+    for (int i = 0; i < MAXB; ++i) {
+        const int j = threadIdx.x + i * NT;
+        if (j < nb) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) v[i][r] = s[j + r * nb];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < MAXB; ++i) {
+        const int j = threadIdx.x + i * NT;
+        if (j < nb) {
+            const int k = j & (Ns - 1);
+            if (Ns > 1) {
+                const int lg = lgNs + 2;
+                v[i][1] = cmul(v[i][1], twiddle(W, wlog, k, lg, inv));
+                v[i][2] = cmul(v[i][2], twiddle(W, wlog, 2 * k, lg, inv));
+                v[i][3] = cmul(v[i][3], twiddle(W, wlog, 3 * k, lg, inv));
+            }
+            const float2 a0 = cadd(v[i][0], v[i][2]);
+            const float2 a1 = csub(v[i][0], v[i][2]);
+            const float2 a2 = cadd(v[i][1], v[i][3]);
+            const float2 d = csub(v[i][1], v[i][3]);
+            // forward: (v1 - v3) * (-i); inverse: (v1 - v3) * (+i)
+            const float2 a3 = inv ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+            const int base = ((j - k) << 2) + k;
+            s[base] = cadd(a0, a2);
+            s[base + Ns] = cadd(a1, a3);
+            s[base + 2 * Ns] = csub(a0, a2);
+            s[base + 3 * Ns] = csub(a1, a3);
+        }
+    }
+    __syncthreads();
+}
+
+// Final radix-2 Stockham stage.
+template <int NT, int MAXB>
+__device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, const float2* __restrict__ W,
+                                         int wlog, bool inv) {
+    const int nb = N >> 1;
+    float2 v[2 * MAXB][2];
+#pragma unroll
+    for (int i = 0; i < 2 * MAXB; ++i) {
+        const int j = threadIdx.x + i * NT;
+        if (j < nb) {
+            v[i][0] = s[j];
+            v[i][1] = s[j + nb];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 2 * MAXB; ++i) {
+        const int j = threadIdx.x + i * NT;
+        if (j < nb) {
+            const int k = j & (Ns - 1);
+            float2 b = v[i][1];
+            if (Ns > 1) b = cmul(b, twiddle(W, wlog, k, lgNs + 1, inv));
+            const int base = ((j - k) << 1) + k;
+            s[base] = cadd(v[i][0], b);
+            s[base + Ns] = csub(v[i][0], b);
+        }
+    }
+    __syncthreads();
+}
+
+// In-place complex FFT of N = 2^logN points in shared memory (unnormalised).
+// Requires N / 4 <= NT * MAXB.  Callers must __syncthreads() before (data
+// written) -- the function ends with a barrier.
+template <int NT, int MAXB>
+__device__ void fft_smem(float2* s, int N, int logN, const float2* __restrict__ W, int wlog, bool inv) {
+    int Ns = 1, lgNs = 0;
+    for (; lgNs + 2 <= logN; lgNs += 2, Ns <<= 2) stage_r4<NT, MAXB>(s, N, Ns, lgNs, W, wlog, inv);
+    if (lgNs < logN) stage_r2<NT, MAXB>(s, N, Ns, lgNs, W, wlog, inv);
+}
+
+// Split post-pass for the pair (k, N-k), 0 <= k <= N/2, on Z = FFT_N(z).
+// Returns X[k] in xk and X[N-k] in xnk (for k == 0: X[0] and X[N]).
+__device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int N, int logN,
+                                           const float2* __restrict__ W, int wlog, float2& xk, float2& xnk) {
+    if (k == 0) {
+        xk = make_float2(zk.x + zk.y, 0.0f);
+        xnk = make_float2(zk.x - zk.y, 0.0f);
+        return;
+    }
+    const float2 E = make_float2(0.5f * (zk.x + znk.x), 0.5f * (zk.y - znk.y));
+    const float2 O = make_float2(0.5f * (zk.y + znk.y), -0.5f * (zk.x - znk.x));
+    const float2 w = twiddle(W, wlog, k, logN + 1, false);   // e^{-i pi k / N}
+    const float2 wO = cmul(w, O);
+    xk = cadd(E, wO);
+    xnk = cconj(csub(E, wO));
+}
+
+// Inverse pre-pass for the pair (k, N-k) from Y[k] (yk) and Y[N-k] (ynk);
+// for k == 0 yk = Y[0], ynk = Y[N] and only zk (= Z'[0]) is meaningful.
+// Imaginary parts of Y[0] and Y[N] are ignored, as FFTW's c2r does.
+__device__ __forceinline__ void irfft_merge(float2 yk, float2 ynk, int k, int N, int logN,
+                                            const float2* __restrict__ W, int wlog, float2& zk, float2& znk) {
+    if (k == 0) {
+        yk.y = 0.0f;
+        ynk.y = 0.0f;
+    }
+    const float2 A = make_float2(yk.x + ynk.x, yk.y - ynk.y);   // Y[k] + conj(Y[N-k])
+    const float2 B = make_float2(yk.x - ynk.x, yk.y + ynk.y);   // Y[k] - conj(Y[N-k])
+    const float2 w = twiddle(W, wlog, k, logN + 1, false);
+    const float2 cB = cmul(cconj(w), B);                          // conj(w^k) B
+    zk = make_float2(A.x - cB.y, A.y + cB.x);                     // A + i conj(w^k) B
+    const float2 wcB = cmul(w, cconj(B));                         // w^k conj(B)
+    znk = make_float2(A.x - wcB.y, -A.y + wcB.x);                 // conj(A) + i w^k conj(B)
+}
+
+}  // namespace pcg

@@ -133,9 +133,9 @@ int pc_run(pc_handle* h, float* output, const float* input, int frame_count);
 int pc_process(pc_handle* h, float* output, const float* input, long long frames, int layout);
 
 /*
- * Same as pc_process with device-resident buffers, enqueued on a caller
- * stream (void* = cudaStream_t; NULL = the handle's own stream).  Returns
- * after enqueueing; the caller synchronises the stream.
+ * Same as pc_process with device-resident buffers, enqueued on the caller's
+ * stream (void* = cudaStream_t; NULL is the CUDA default stream, as in every
+ * CUDA API).  Returns after enqueueing; the caller synchronises the stream.
  */
 int pc_process_device(pc_handle* h, float* d_output, const float* d_input, long long frames,
                       int layout, void* stream);
@@ -167,7 +167,8 @@ long long pc_kernel_launches(const pc_handle* h);
 
 /* Per-kernel timing record filled by pc_profile_kernels. */
 typedef struct pc_kernel_stats {
-    char name[32];         /* "fire_small", "fire_mid", "fire_large", "spread_mac" */
+    char name[32];         /* "step_small", "step_mid", "step_large": the step kernel of
+                              block-size class N <= 1024, <= 4096, <= 16384 */
     long long launches;    /* launches that had work in their phase */
     double total_ms;       /* CUDA-event time summed over those launches */
     double alg_bytes;      /* algorithmic bytes those launches had to move */

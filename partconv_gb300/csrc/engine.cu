@@ -6,10 +6,12 @@
 // validation and IR partitioning (src/partconv.cpp:70-230), device-resident
 // FDL state, and the per-callback schedule.  The reference's pthread level
 // workers become a static per-phase task table: the level schedule repeats
-// every H = max_L N_L / N0 base steps, so for each phase the host lists the
-// level blocks that fire and the MAC slices that are spread over the steps
-// between a level's blocks.  Each base step is one launch per kernel class;
-// batches of steps are replayed from a captured CUDA graph.
+// every H = max_L N_L / N0 base steps, so for each phase and kernel class the
+// host lists the level blocks that fire and the MAC slices spread over the
+// steps between a level's blocks.  A base step is one launch per kernel
+// class that has work in that phase (level 0 fires every step, so its class
+// always runs); batches of steps replay a captured CUDA graph whose nodes
+// have their phase baked in.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,8 +33,9 @@ using namespace pcg;
 namespace {
 
 constexpr int kWlog = 15;          // twiddle table 2^15 entries: real FFTs up to 2 * 16384
-constexpr int kGraphSteps = 64;    // base steps per captured graph
+constexpr int kMinGraphSteps = 64; // base steps per captured graph (a multiple of the hyperperiod)
 constexpr int kMinN0 = 16;
+constexpr int kClasses = 3;
 
 bool is_pow2(long x) { return x > 0 && (x & (x - 1)) == 0; }
 int ilog2(long x) {
@@ -127,6 +130,7 @@ struct pc_handle {
     bool ready = false;
     int device = -1;
     cudaStream_t stream = nullptr;
+    cudaStream_t side[kClasses] = {nullptr, nullptr, nullptr};   // graph-capture branches
 
     int fs = 0, N0 = 0, n_in = 0, n_out = 0;
     int relaxed = 0;
@@ -140,17 +144,16 @@ struct pc_handle {
     std::vector<DevPC> h_pcs;
     std::vector<DevLevel> h_lv;
     Bank bank{};
-    int H = 1;
+    int H = 1;        // hyperperiod (steps)
+    int G = 64;       // steps per captured graph (multiple of H)
     int maxN = 0;
+    int l0_class = 0;
 
-    // per-phase tables (device) and launch shapes
-    FireTask* d_fire[3] = {nullptr, nullptr, nullptr};
-    int* d_fire_off[3] = {nullptr, nullptr, nullptr};
-    int fire_grid[3] = {0, 0, 0};
-    int fire_maxN[3] = {0, 0, 0};
-    SpreadTask* d_spread = nullptr;
-    int* d_spread_off = nullptr;
-    int spread_grid = 0;
+    // per (class, phase) task lists: d_tasks + off[cls][phase], count cnt[cls][phase]
+    Task* d_tasks = nullptr;
+    std::vector<int> off[kClasses], cnt[kClasses];
+    std::vector<double> alg_bytes[kClasses];
+    int class_maxN[kClasses] = {0, 0, 0};
     RunState* d_rs = nullptr;
 
     // run() staging and Relaxed carry (planar [n_out][N0])
@@ -166,11 +169,7 @@ struct pc_handle {
     size_t rtmp_cap = 0;
 
     cudaGraphExec_t gexec = nullptr;
-    int graph_launches_per_replay = 0;
-
-    // algorithmic bytes per phase (profiling)
-    std::vector<double> fire_bytes[3];
-    std::vector<double> spread_bytes;
+    long long graph_kernels = 0;   // kernel nodes per replay
 
     long long frame_num = 0;
     long long launches = 0;
@@ -187,9 +186,9 @@ int cuda_fail(pc_handle* h, cudaError_t e, const char* where) {
     return fail(h, PC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(call, where)                                   \
-    do {                                                  \
-        cudaError_t e_ = (call);                          \
+#define CK(call, where)                                        \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
         if (e_ != cudaSuccess) return cuda_fail(h, e_, where); \
     } while (0)
 
@@ -204,46 +203,77 @@ void free_device(pc_handle* h) {
     if (h->d_rtmp) cudaFree(h->d_rtmp);
     h->d_big_in = h->d_big_out = h->d_rtmp = nullptr;
     h->big_in_cap = h->big_out_cap = h->rtmp_cap = 0;
+    for (auto& s : h->side) {
+        if (s) cudaStreamDestroy(s);
+        s = nullptr;
+    }
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     h->ready = false;
 }
 
-// Launch one base step (every kernel class that has work in some phase).
-int launch_step(pc_handle* h, const RunState& rs, const RunState* rs_dev, int s, cudaStream_t st) {
-    for (int cls = 0; cls < 3; ++cls) {
-        if (h->fire_grid[cls] <= 0) continue;
-        CK(launch_fire(cls, h->fire_grid[cls], h->fire_maxN[cls], h->bank, h->d_fire[cls], h->d_fire_off[cls], rs,
-                       rs_dev, s, st),
-           "fire kernel launch");
+int phase_of(const pc_handle* h, long long step) { return (int)(step & (long long)(h->H - 1)); }
+
+// One base step by direct launches (classes with work in this phase).
+int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st) {
+    const int ph = phase_of(h, rs.step_base);
+    for (int k = 0; k < kClasses; ++k) {
+        const int cls = (h->l0_class + k) % kClasses;   // level-0 class first
+        const int n = h->cnt[cls][ph];
+        if (n <= 0) continue;
+        CK(launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs, nullptr, 0, st),
+           "step launch");
+        h->launches += 1;
     }
-    CK(launch_spread(h->spread_grid, h->bank, h->d_spread, h->d_spread_off, rs, rs_dev, s, st), "spread launch");
     return PC_OK;
 }
 
-int kernels_per_step(const pc_handle* h) {
-    int n = 0;
-    for (int cls = 0; cls < 3; ++cls) n += h->fire_grid[cls] > 0;
-    return n + (h->spread_grid > 0);
-}
-
+// Capture G steps starting at a step with phase 0.  Classes other than the
+// level-0 class run on side branches joined at the end of their step.
 int build_graph(pc_handle* h) {
     cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    std::vector<cudaEvent_t> evs;
+    auto mk = [&]() {
+        cudaEvent_t e;
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        evs.push_back(e);
+        return e;
+    };
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(h, e, "begin capture");
     RunState dummy{};
-    for (int s = 0; s < kGraphSteps; ++s) {
-        int r = launch_step(h, dummy, h->d_rs, s, h->stream);
-        if (r) {
-            cudaStreamEndCapture(h->stream, &g);
-            if (g) cudaGraphDestroy(g);
-            return r;
+    long long kernels = 0;
+    for (int s = 0; s < h->G && e == cudaSuccess; ++s) {
+        const int ph = s & (h->H - 1);
+        std::vector<cudaEvent_t> joins;
+        for (int cls = 0; cls < kClasses && e == cudaSuccess; ++cls) {
+            if (cls == h->l0_class || h->cnt[cls][ph] <= 0) continue;
+            cudaEvent_t fork = mk();
+            e = cudaEventRecord(fork, h->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side[cls], fork, 0);
+            if (e == cudaSuccess)
+                e = launch_step_class(cls, h->cnt[cls][ph], h->class_maxN[cls], h->bank,
+                                      h->d_tasks + h->off[cls][ph], dummy, h->d_rs, s, h->side[cls]);
+            cudaEvent_t join = mk();
+            if (e == cudaSuccess) e = cudaEventRecord(join, h->side[cls]);
+            joins.push_back(join);
+            ++kernels;
         }
+        const int c0 = h->l0_class;
+        if (e == cudaSuccess)
+            e = launch_step_class(c0, h->cnt[c0][ph], h->class_maxN[c0], h->bank, h->d_tasks + h->off[c0][ph], dummy,
+                                  h->d_rs, s, h->stream);
+        ++kernels;
+        for (auto j : joins)
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, j, 0);
     }
-    CK(cudaStreamEndCapture(h->stream, &g), "end capture");
-    cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(h, e, "graph instantiate");
-    h->graph_launches_per_replay = kGraphSteps * kernels_per_step(h);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    for (auto ev : evs) cudaEventDestroy(ev);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->gexec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph capture");
+    h->graph_kernels = kernels;
     return PC_OK;
 }
 
@@ -267,6 +297,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     CK(cudaGetDevice(&dev), "cudaGetDevice");
     h->device = dev;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream create");
+    for (auto& s : h->side) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream create");
     CK(prepare_kernels(), "kernel attributes");
 
     h->fs = fs;
@@ -277,7 +308,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     const int N0 = buffer_size;
     const int npc = (int)h->specs.size();
 
-    // ---- sizes and offsets -------------------------------------------------
     int nlv = 0, maxN = 0, Hh = 1;
     for (auto& p : h->specs) {
         nlv += (int)p.N.size();
@@ -285,10 +315,12 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         Hh = std::max(Hh, p.N.back() / N0);
     }
     h->H = Hh;
+    h->G = std::max(Hh, kMinGraphSteps);
     h->maxN = maxN;
+    h->l0_class = fire_class_of(N0);
 
+    // ---- arena layout --------------------------------------------------------------
     Carve cv;
-    // static region
     const size_t off_W = cv.take(sizeof(float2) << kWlog);
     const size_t off_pcs = cv.take(sizeof(DevPC) * npc);
     const size_t off_lv = cv.take(sizeof(DevLevel) * nlv);
@@ -299,7 +331,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             for (size_t L = 0; L < p.N.size(); ++L, ++li)
                 off_H[li] = cv.take(sizeof(float2) * (size_t)p.P[L] * (p.N[L] + 2));
     }
-    // mixing lists
     std::vector<std::vector<int>> out_list(n_out);
     for (int i = 0; i < npc; ++i)
         if (!h->specs[i].mute) out_list[h->specs[i].out_ch].push_back(i);
@@ -312,100 +343,188 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     const size_t off_out_off = cv.take(sizeof(int) * (n_out + 1));
     const size_t off_out_pcs = cv.take(sizeof(int) * std::max<size_t>(1, out_pcs.size()));
     const size_t off_zero = cv.take(sizeof(int) * std::max<size_t>(1, zero_list.size()));
-
-    // task tables
-    std::vector<std::vector<FireTask>> fire(3);
-    std::vector<std::vector<int>> fire_off(3, std::vector<int>(Hh + 1, 0));
-    std::vector<SpreadTask> spread;
-    std::vector<int> spread_off(Hh + 1, 0);
-    {
-        struct LvInfo { int gidx, N, P, T, sb, cs, M, L; };
-        std::vector<LvInfo> all;
-        int li = 0;
-        for (auto& p : h->specs) {
-            long s = 0;
-            for (size_t L = 0; L < p.N.size(); ++L, ++li) {
-                all.push_back({li, p.N[L], p.P[L], p.N[L] / N0, (int)(s / N0), p.N[L] + 2, (int)p.N.size(), (int)L});
-                s += (long)p.N[L] * p.P[L];
-            }
-        }
-        for (int cls = 0; cls < 3; ++cls) h->fire_bytes[cls].assign(Hh, 0.0);
-        h->spread_bytes.assign(Hh, 0.0);
-        // bytes a fire task must move: spectra rows read/written, the
-        // 2N-sample window read and N samples written (level 0 also reads the
-        // other levels' due slices and appends N0 samples to the input ring)
-        auto fire_bytes = [&](const LvInfo& l) {
-            const double C = l.N + 1.0;
-            double b = (l.T == 1 ? 8.0 * C * 2.0 * l.P : 24.0 * C) + 12.0 * l.N;
-            if (l.L == 0) b += 4.0 * N0 * (l.M - 1) + 4.0 * N0;
-            return b;
-        };
-        std::vector<LvInfo> order = all;
-        std::stable_sort(order.begin(), order.end(), [](const LvInfo& a, const LvInfo& b) { return a.N > b.N; });
-        for (int g = 0; g < Hh; ++g) {
-            for (auto& l : order) {
-                if ((g + 1 + l.sb) % l.T == 0) {
-                    fire[fire_class_of(l.N)].push_back({l.gidx});
-                    h->fire_bytes[fire_class_of(l.N)][g] += fire_bytes(l);
-                }
-            }
-            for (int cls = 0; cls < 3; ++cls) fire_off[cls][g + 1] = (int)fire[cls].size();
-            for (auto& l : all) {
-                if (l.T < 2 || l.P < 2) continue;
-                const int phi = (g + 1 + l.sb) % l.T;
-                if (phi == 0) continue;
-                const int j = phi - 1, nch = l.T - 1;
-                const int lo = (int)(((long)j * l.cs / nch) & ~1L);
-                const int hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
-                for (int k0 = lo; k0 < hi; k0 += 2 * kSpreadNT)
-                    spread.push_back({l.gidx, k0, std::min(hi, k0 + 2 * kSpreadNT)});
-                h->spread_bytes[g] += (16.0 * (l.P - 1) + 8.0) * (hi - lo);
-            }
-            spread_off[g + 1] = (int)spread.size();
-        }
-    }
-    size_t off_fire[3], off_fire_off[3];
-    for (int cls = 0; cls < 3; ++cls) {
-        off_fire[cls] = cv.take(sizeof(FireTask) * std::max<size_t>(1, fire[cls].size()));
-        off_fire_off[cls] = cv.take(sizeof(int) * (Hh + 1));
-    }
-    const size_t off_spread = cv.take(sizeof(SpreadTask) * std::max<size_t>(1, spread.size()));
-    const size_t off_spread_off = cv.take(sizeof(int) * (Hh + 1));
     const size_t off_rs = cv.take(sizeof(RunState));
     const size_t off_in1 = cv.take(sizeof(float) * (size_t)N0 * n_in);
     const size_t off_out1 = cv.take(sizeof(float) * (size_t)N0 * n_out);
+    // task table size is known only after enumeration; it goes last in the static part
+    const size_t off_tasks_placeholder = cv.off;
+    (void)off_tasks_placeholder;
 
-    // state region (zeroed by reset)
-    const size_t state_begin = cv.take(0);
-    std::vector<size_t> off_xring(npc), off_pcout(npc);
-    std::vector<int> rin(npc);
+    // state (zeroed by reset), laid out after the task table below
+    struct StateOffsets {
+        std::vector<size_t> xring, pcout, X, Yp, yr;
+        size_t mix = 0, carry = 0;
+    } so;
+    std::vector<int> rin(npc), rl(nlv);
     for (int i = 0; i < npc; ++i) {
         long r = 1;
         while (r < 2L * h->specs[i].N.back()) r <<= 1;
         rin[i] = (int)r;
-        off_xring[i] = cv.take(sizeof(float) * r);
-        off_pcout[i] = cv.take(sizeof(float) * N0);
     }
-    std::vector<size_t> off_X(nlv), off_Yp(nlv), off_yr(nlv);
-    std::vector<int> rl(nlv);
     {
         int li = 0;
         for (auto& p : h->specs) {
             long s = 0;
             for (size_t L = 0; L < p.N.size(); ++L, ++li) {
-                const size_t cs = p.N[L] + 2;
-                off_X[li] = cv.take(sizeof(float2) * p.P[L] * cs);
-                off_Yp[li] = cv.take(sizeof(float2) * cs);
                 long r = p.N[L];
                 while (r < s + N0) r <<= 1;
                 rl[li] = (int)r;
-                off_yr[li] = cv.take(sizeof(float) * r);
                 s += (long)p.N[L] * p.P[L];
             }
         }
     }
-    const size_t off_mix = cv.take(sizeof(int) * n_out);
-    const size_t off_carry = cv.take(sizeof(float) * (size_t)N0 * n_out);
+
+    // ---- descriptors (host) ----------------------------------------------------------
+    h->h_pcs.assign(npc, DevPC{});
+    h->h_lv.assign(nlv, DevLevel{});
+    {
+        int li = 0;
+        for (int i = 0; i < npc; ++i) {
+            PCSpec& p = h->specs[i];
+            DevPC& d = h->h_pcs[i];
+            d.M = (int)p.N.size();
+            d.lv0 = li;
+            d.in_ch = p.in_ch;
+            d.out_ch = p.out_ch;
+            d.mute = p.mute;
+            d.mix_mode = p.mute ? 0 : (out_list[p.out_ch].size() == 1 ? 1 : 2);
+            d.zero_outs = (i == 0) ? (int)zero_list.size() : 0;
+            d.zero_off = 0;
+            d.scale = p.scale;
+            d.rin_mask = rin[i] - 1;
+            long s = 0;
+            for (size_t L = 0; L < p.N.size(); ++L, ++li) {
+                DevLevel& l = h->h_lv[li];
+                l.N = p.N[L];
+                l.logN = ilog2(p.N[L]);
+                l.P = p.P[L];
+                l.T = p.N[L] / N0;
+                l.s_blocks = (int)(s / N0);
+                l.cs = p.N[L] + 2;
+                l.rmask = rl[li] - 1;
+                l.pc = i;
+                s += (long)p.N[L] * p.P[L];
+            }
+        }
+    }
+
+    // ---- per (class, phase) task lists ------------------------------------------------
+    // Tasks point into the arena, so they are built after the state offsets
+    // are known; first count them to size the table.
+    std::vector<std::vector<std::vector<Task>>> lists(kClasses, std::vector<std::vector<Task>>(Hh));
+    auto spread_bins = [&](int cls) { return 2 * class_threads(cls); };
+    for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(Hh, 0.0);
+    // order: larger fires first (longest CTAs start first), then level-0
+    // fires, then spread tasks
+    std::vector<int> order(nlv);
+    for (int i = 0; i < nlv; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h->h_lv[a].N > h->h_lv[b].N; });
+    for (int g = 0; g < Hh; ++g) {
+        for (int li : order) {
+            const DevLevel& l = h->h_lv[li];
+            if ((g + 1 + l.s_blocks) % l.T) continue;
+            const DevPC& d = h->h_pcs[l.pc];
+            Task t{};
+            t.kind = 0;
+            t.N = l.N;
+            t.logN = l.logN;
+            t.P = l.P;
+            t.T = l.T;
+            t.s_blocks = l.s_blocks;
+            t.cs = l.cs;
+            t.rmask = l.rmask;
+            t.M = d.M;
+            t.in_ch = d.in_ch;
+            t.out_ch = d.out_ch;
+            t.mix_mode = d.mix_mode;
+            t.zero_outs = (l.T == 1) ? d.zero_outs : 0;
+            t.zero_off = d.zero_off;
+            t.rin_mask = d.rin_mask;
+            t.lv_index = li;
+            t.scale = d.scale;
+            const int cls = fire_class_of(l.N);
+            lists[cls][g].push_back(t);
+            // bytes a fire must move: H0 row read, new X row written, the
+            // partial-sum row read (level 0 also X_{b-1} and H_1 rows), the
+            // 2N-sample window read, N samples written; level 0 also reads
+            // the other levels' due slices and appends N0 input samples
+            const double C = l.N + 1.0;
+            double b = 8.0 * C * 2.0 + 12.0 * l.N;
+            if (l.T == 1) {
+                b += 8.0 * C * (l.P >= 2 ? 2.0 : 0.0) + (l.P >= 3 ? 8.0 * C : 0.0);
+                b += 4.0 * N0 * (d.M - 1) + 4.0 * N0;
+            } else if (l.P >= 2) {
+                b += 8.0 * C;
+            }
+            h->alg_bytes[cls][g] += b;
+        }
+        const int sc = h->l0_class;
+        for (int li = 0; li < nlv; ++li) {
+            const DevLevel& l = h->h_lv[li];
+            int lo, hi, p_lo;
+            if (l.T == 1) {
+                if (l.P < 3) continue;
+                lo = 0;
+                hi = l.cs;
+                p_lo = 2;
+            } else {
+                if (l.P < 2) continue;
+                const int phi = (g + 1 + l.s_blocks) % l.T;
+                if (phi == 0) continue;
+                const int j = phi - 1, nch = l.T - 1;
+                lo = (int)(((long)j * l.cs / nch) & ~1L);
+                hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
+                p_lo = 1;
+            }
+            for (int k0 = lo; k0 < hi; k0 += spread_bins(sc)) {
+                Task t{};
+                t.kind = 1;
+                t.N = l.N;
+                t.P = l.P;
+                t.T = l.T;
+                t.s_blocks = l.s_blocks;
+                t.cs = l.cs;
+                t.k0 = k0;
+                t.k1 = std::min(hi, k0 + spread_bins(sc));
+                t.p_lo = p_lo;
+                t.lv_index = li;
+                lists[sc][g].push_back(t);
+            }
+            h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0) * (hi - lo);
+        }
+    }
+    size_t ntasks = 0;
+    for (int cls = 0; cls < kClasses; ++cls) {
+        h->off[cls].assign(Hh + 1, 0);
+        h->cnt[cls].assign(Hh, 0);
+        for (int g = 0; g < Hh; ++g) {
+            h->off[cls][g] = (int)ntasks;
+            h->cnt[cls][g] = (int)lists[cls][g].size();
+            ntasks += lists[cls][g].size();
+        }
+        h->off[cls][Hh] = (int)ntasks;
+    }
+    const size_t off_tasks = cv.take(sizeof(Task) * std::max<size_t>(1, ntasks));
+
+    // state region
+    const size_t state_begin = cv.take(0);
+    so.xring.resize(npc);
+    so.pcout.resize(npc);
+    for (int i = 0; i < npc; ++i) {
+        so.xring[i] = cv.take(sizeof(float) * rin[i]);
+        so.pcout[i] = cv.take(sizeof(float) * N0);
+    }
+    so.X.resize(nlv);
+    so.Yp.resize(nlv);
+    so.yr.resize(nlv);
+    for (int li = 0; li < nlv; ++li) {
+        const DevLevel& l = h->h_lv[li];
+        so.X[li] = cv.take(sizeof(float2) * (size_t)l.P * l.cs);
+        so.Yp[li] = cv.take(sizeof(float2) * 2 * (size_t)l.cs);
+        so.yr[li] = cv.take(sizeof(float) * (size_t)(l.rmask + 1));
+    }
+    so.mix = cv.take(sizeof(int) * n_out);
+    so.carry = cv.take(sizeof(float) * (size_t)N0 * n_out);
     const size_t state_end = cv.take(0);
 
     h->arena_bytes = cv.off;
@@ -420,6 +539,51 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->state_bytes = state_end - state_begin;
     CK(cudaMemsetAsync(A + state_begin, 0, h->state_bytes, h->stream), "memset state");
 
+    // pointers into the arena
+    for (int i = 0; i < npc; ++i) {
+        h->h_pcs[i].xring = reinterpret_cast<float*>(A + so.xring[i]);
+        h->h_pcs[i].pcout = reinterpret_cast<float*>(A + so.pcout[i]);
+    }
+    for (int li = 0; li < nlv; ++li) {
+        DevLevel& l = h->h_lv[li];
+        l.H = reinterpret_cast<float2*>(A + off_H[li]);
+        l.X = reinterpret_cast<float2*>(A + so.X[li]);
+        l.Yp = reinterpret_cast<float2*>(A + so.Yp[li]);
+        l.yring = reinterpret_cast<float*>(A + so.yr[li]);
+    }
+    std::vector<Task> all_tasks;
+    all_tasks.reserve(ntasks);
+    for (int cls = 0; cls < kClasses; ++cls)
+        for (int g = 0; g < Hh; ++g)
+            for (Task t : lists[cls][g]) {
+                const DevLevel& l = h->h_lv[t.lv_index];
+                const DevPC& d = h->h_pcs[l.pc];
+                t.H = l.H;
+                t.X = l.X;
+                t.Yp = l.Yp;
+                t.yring = l.yring;
+                t.xring = d.xring;
+                t.pcout = d.pcout;
+                if (t.kind == 0 && t.T == 1)
+                    for (int L = 1; L <= kEmitLevels && L < d.M; ++L) {
+                        t.eyring[L - 1] = h->h_lv[d.lv0 + L].yring;
+                        t.emask[L - 1] = h->h_lv[d.lv0 + L].rmask;
+                    }
+                all_tasks.push_back(t);
+            }
+    h->d_tasks = reinterpret_cast<Task*>(A + off_tasks);
+    if (!all_tasks.empty())
+        CK(cudaMemcpyAsync(h->d_tasks, all_tasks.data(), sizeof(Task) * all_tasks.size(), cudaMemcpyHostToDevice,
+                           h->stream),
+           "upload tasks");
+    for (int cls = 0; cls < kClasses; ++cls) h->class_maxN[cls] = 0;
+    for (auto& l : h->h_lv) {
+        const int cls = fire_class_of(l.N);
+        h->class_maxN[cls] = std::max(h->class_maxN[cls], l.N);
+    }
+    // the level-0 class also runs spread tasks; its smem must fit its fires
+    if (h->class_maxN[h->l0_class] == 0) h->class_maxN[h->l0_class] = N0;
+
     // twiddles, computed in double
     {
         std::vector<float2> W((size_t)1 << kWlog);
@@ -430,48 +594,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         CK(cudaMemcpyAsync(A + off_W, W.data(), sizeof(float2) * W.size(), cudaMemcpyHostToDevice, h->stream),
            "upload twiddles");
         CK(cudaStreamSynchronize(h->stream), "sync");
-    }
-
-    // descriptors
-    h->h_pcs.assign(npc, DevPC{});
-    h->h_lv.assign(nlv, DevLevel{});
-    std::vector<int> zero_owner_count(npc, 0);
-    if (!zero_list.empty()) zero_owner_count[0] = (int)zero_list.size();
-    {
-        int li = 0;
-        for (int i = 0; i < npc; ++i) {
-            PCSpec& p = h->specs[i];
-            DevPC& d = h->h_pcs[i];
-            d.M = (int)p.N.size();
-            d.lv0 = li;
-            d.in_ch = p.in_ch;
-            d.out_ch = p.out_ch;
-            d.mute = p.mute;
-            d.mix_mode = p.mute ? 0 : (out_list[p.out_ch].size() == 1 ? 1 : 2);
-            d.zero_outs = zero_owner_count[i];
-            d.zero_off = 0;
-            d.scale = p.scale;
-            d.rin_mask = rin[i] - 1;
-            d.xring = reinterpret_cast<float*>(A + off_xring[i]);
-            d.pcout = reinterpret_cast<float*>(A + off_pcout[i]);
-            long s = 0;
-            for (size_t L = 0; L < p.N.size(); ++L, ++li) {
-                DevLevel& l = h->h_lv[li];
-                l.N = p.N[L];
-                l.logN = ilog2(p.N[L]);
-                l.P = p.P[L];
-                l.T = p.N[L] / N0;
-                l.s_blocks = (int)(s / N0);
-                l.cs = p.N[L] + 2;
-                l.rmask = rl[li] - 1;
-                l.pc = i;
-                l.H = reinterpret_cast<float2*>(A + off_H[li]);
-                l.X = reinterpret_cast<float2*>(A + off_X[li]);
-                l.Yp = reinterpret_cast<float2*>(A + off_Yp[li]);
-                l.yring = reinterpret_cast<float*>(A + off_yr[li]);
-                s += (long)p.N[L] * p.P[L];
-            }
-        }
     }
     CK(cudaMemcpyAsync(A + off_pcs, h->h_pcs.data(), sizeof(DevPC) * npc, cudaMemcpyHostToDevice, h->stream),
        "upload PCs");
@@ -488,71 +610,37 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         CK(cudaMemcpyAsync(A + off_zero, zero_list.data(), sizeof(int) * zero_list.size(), cudaMemcpyHostToDevice,
                            h->stream),
            "upload zero list");
-    for (int cls = 0; cls < 3; ++cls) {
-        h->d_fire[cls] = reinterpret_cast<FireTask*>(A + off_fire[cls]);
-        h->d_fire_off[cls] = reinterpret_cast<int*>(A + off_fire_off[cls]);
-        if (!fire[cls].empty())
-            CK(cudaMemcpyAsync(h->d_fire[cls], fire[cls].data(), sizeof(FireTask) * fire[cls].size(),
-                               cudaMemcpyHostToDevice, h->stream),
-               "upload fire tasks");
-        CK(cudaMemcpyAsync(h->d_fire_off[cls], fire_off[cls].data(), sizeof(int) * (Hh + 1), cudaMemcpyHostToDevice,
-                           h->stream),
-           "upload fire offsets");
-        int g = 0;
-        for (int ph = 0; ph < Hh; ++ph) g = std::max(g, fire_off[cls][ph + 1] - fire_off[cls][ph]);
-        h->fire_grid[cls] = g;
-        h->fire_maxN[cls] = 0;
-    }
-    for (auto& p : h->specs)
-        for (int n : p.N) {
-            int cls = fire_class_of(n);
-            h->fire_maxN[cls] = std::max(h->fire_maxN[cls], n);
-        }
-    h->d_spread = reinterpret_cast<SpreadTask*>(A + off_spread);
-    h->d_spread_off = reinterpret_cast<int*>(A + off_spread_off);
-    if (!spread.empty())
-        CK(cudaMemcpyAsync(h->d_spread, spread.data(), sizeof(SpreadTask) * spread.size(), cudaMemcpyHostToDevice,
-                           h->stream),
-           "upload spread tasks");
-    CK(cudaMemcpyAsync(h->d_spread_off, spread_off.data(), sizeof(int) * (Hh + 1), cudaMemcpyHostToDevice,
-                       h->stream),
-       "upload spread offsets");
-    {
-        int g = 0;
-        for (int ph = 0; ph < Hh; ++ph) g = std::max(g, spread_off[ph + 1] - spread_off[ph]);
-        h->spread_grid = g;
-    }
     h->d_rs = reinterpret_cast<RunState*>(A + off_rs);
     h->d_in1 = reinterpret_cast<float*>(A + off_in1);
     h->d_out1 = reinterpret_cast<float*>(A + off_out1);
-    h->d_carry = reinterpret_cast<float*>(A + off_carry);
+    h->d_carry = reinterpret_cast<float*>(A + so.carry);
 
     h->bank.pcs = reinterpret_cast<const DevPC*>(A + off_pcs);
     h->bank.lv = reinterpret_cast<const DevLevel*>(A + off_lv);
     h->bank.W = reinterpret_cast<const float2*>(A + off_W);
     h->bank.wlog = kWlog;
     h->bank.N0 = N0;
-    h->bank.H = Hh;
     h->bank.n_out = n_out;
     h->bank.out_off = reinterpret_cast<const int*>(A + off_out_off);
     h->bank.out_pcs = reinterpret_cast<const int*>(A + off_out_pcs);
-    h->bank.mix_cnt = reinterpret_cast<int*>(A + off_mix);
+    h->bank.mix_cnt = reinterpret_cast<int*>(A + so.mix);
     h->bank.zero_list = reinterpret_cast<const int*>(A + off_zero);
 
-    // ---- filter spectra: one CTA per (PC, level, part) row -------------------
+    // ---- filter spectra: one CTA per (PC, level, part) row -------------------------------
     {
         std::vector<float*> d_irs(npc, nullptr);
-        std::vector<std::vector<SpectraJob>> jobs(3);
-        for (int i = 0; i < npc; ++i) {
+        std::vector<std::vector<SpectraJob>> jobs(kClasses);
+        int rc = PC_OK;
+        for (int i = 0; i < npc && rc == PC_OK; ++i) {
             PCSpec& p = h->specs[i];
             e = cudaMalloc(&d_irs[i], sizeof(float) * std::max<size_t>(1, p.ir.size()));
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_irs[i], p.ir.data(), sizeof(float) * p.ir.size(), cudaMemcpyHostToDevice,
+                                    h->stream);
             if (e != cudaSuccess) {
-                for (auto q : d_irs)
-                    if (q) cudaFree(q);
-                free_device(h);
-                return fail(h, PC_ERR_NOMEM, "device allocation for the IR failed");
+                rc = fail(h, PC_ERR_NOMEM, std::string("IR upload failed: ") + cudaGetErrorString(e));
+                break;
             }
-            cudaMemcpyAsync(d_irs[i], p.ir.data(), sizeof(float) * p.ir.size(), cudaMemcpyHostToDevice, h->stream);
             long s = 0;
             for (size_t L = 0; L < p.N.size(); ++L) {
                 const DevLevel& l = h->h_lv[h->h_pcs[i].lv0 + L];
@@ -569,9 +657,8 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 s += (long)l.N * l.P;
             }
         }
-        std::vector<SpectraJob*> d_jobs(3, nullptr);
-        int rc = PC_OK;
-        for (int cls = 0; cls < 3 && rc == PC_OK; ++cls) {
+        std::vector<SpectraJob*> d_jobs(kClasses, nullptr);
+        for (int cls = 0; cls < kClasses && rc == PC_OK; ++cls) {
             if (jobs[cls].empty()) continue;
             int mN = 0;
             for (auto& j : jobs[cls]) mN = std::max(mN, j.N);
@@ -589,26 +676,27 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             if (q) cudaFree(q);
         for (auto q : d_jobs)
             if (q) cudaFree(q);
+        if (rc == PC_OK && se != cudaSuccess) rc = cuda_fail(h, se, "filter spectra");
         if (rc) {
+            std::string m = h->err;
             free_device(h);
+            h->err = m;
             return rc;
-        }
-        if (se != cudaSuccess) {
-            free_device(h);
-            return cuda_fail(h, se, "filter spectra");
         }
     }
 
     int r = build_graph(h);
     if (r) {
+        std::string m = h->err;
         free_device(h);
+        h->err = m;
         return r;
     }
     h->frame_num = 0;
     h->ready = true;
     if (h->verbosity > 0) {
-        printf("partconv_gb300: %d PCs, N0 = %d, hyperperiod %d steps, %.1f MB device\n", npc, N0, Hh,
-               h->arena_bytes / 1e6);
+        printf("partconv_gb300: %d PCs, N0 = %d, hyperperiod %d steps, %zu tasks, %.1f MB device\n", npc, N0, Hh,
+               ntasks, h->arena_bytes / 1e6);
         for (int i = 0; i < npc; ++i) {
             printf("  PC %d: ", i);
             for (size_t L = 0; L < h->specs[i].N.size(); ++L)
@@ -641,24 +729,33 @@ IOView make_view(const pc_handle* h, const float* in, float* out, long long fram
     return v;
 }
 
-// Run nsteps base steps starting at h->frame_num through the view.
+// Run nsteps base steps starting at h->frame_num through the view: direct
+// launches up to the next graph boundary, graph replays, direct remainder.
 int run_steps(pc_handle* h, const IOView& view, long long nsteps, cudaStream_t st) {
     long long done = 0;
     RunState rs;
     rs.io = view;
-    while (nsteps - done >= kGraphSteps && h->gexec) {
+    auto direct = [&](long long upto) -> int {
+        for (; done < upto; ++done) {
+            rs.step_base = h->frame_num + done;
+            int r = launch_step_direct(h, rs, st);
+            if (r) return r;
+        }
+        return PC_OK;
+    };
+    const long long G = h->G;
+    const long long misalign = (G - (h->frame_num % G)) % G;
+    int r = direct(std::min(nsteps, misalign));
+    if (r) return r;
+    while (nsteps - done >= G && h->gexec) {
         rs.step_base = h->frame_num + done;
         CK(launch_set_state(h->d_rs, rs, st), "state launch");
         CK(cudaGraphLaunch(h->gexec, st), "graph launch");
-        h->launches += 1 + h->graph_launches_per_replay;
-        done += kGraphSteps;
+        h->launches += 1 + h->graph_kernels;
+        done += G;
     }
-    for (; done < nsteps; ++done) {
-        rs.step_base = h->frame_num + done;
-        int r = launch_step(h, rs, nullptr, 0, st);
-        if (r) return r;
-        h->launches += kernels_per_step(h);
-    }
+    r = direct(nsteps);
+    if (r) return r;
     h->frame_num += nsteps;
     return PC_OK;
 }
@@ -866,8 +963,7 @@ int pc_process(pc_handle* h, float* output, const float* input, long long frames
 int pc_process_device(pc_handle* h, float* d_output, const float* d_input, long long frames, int layout,
                       void* stream) {
     if (!h) return PC_ERR_ARG;
-    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
-    return process_device_impl(h, d_output, d_input, frames, layout, st);
+    return process_device_impl(h, d_output, d_input, frames, layout, (cudaStream_t)stream);
 }
 
 int pc_reset(pc_handle* h) {
@@ -907,7 +1003,8 @@ int pc_get_info(const pc_handle* h, pc_info* info) {
     info->relaxed = h->relaxed;
     info->hyperperiod = h->H;
     info->frame_num = h->frame_num;
-    info->device_bytes = (long long)h->arena_bytes + (long long)sizeof(float) * (h->big_in_cap + h->big_out_cap + h->rtmp_cap);
+    info->device_bytes =
+        (long long)h->arena_bytes + (long long)sizeof(float) * (h->big_in_cap + h->big_out_cap + h->rtmp_cap);
     return PC_OK;
 }
 
@@ -929,8 +1026,12 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     if (!h->ready) return fail(h, PC_ERR_STATE, "profile before setup");
     if (nsteps < 1 || !out || max_kinds < 1) return fail(h, PC_ERR_ARG, "bad profile arguments");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
-    static const char* names[4] = {"fire_small", "fire_mid", "fire_large", "spread_mac"};
-    struct Rec { int kind; int phase; cudaEvent_t a, b; };
+    static const char* names[kClasses] = {"step_small", "step_mid", "step_large"};
+    struct Rec {
+        int cls;
+        int phase;
+        cudaEvent_t a, b;
+    };
     std::vector<Rec> recs;
     // every step reads the staging input block and writes the staging output
     IOView v = make_view(h, h->d_in1, h->d_out1, h->N0, PC_INTERLEAVED, 0);
@@ -941,18 +1042,17 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     int rc = PC_OK;
     for (long long s = 0; s < nsteps && rc == PC_OK; ++s) {
         rs.step_base = h->frame_num + s;
-        const int phase = (int)(rs.step_base & (h->H - 1));
-        for (int kind = 0; kind < 4 && rc == PC_OK; ++kind) {
-            const int grid = kind < 3 ? h->fire_grid[kind] : h->spread_grid;
-            if (grid <= 0) continue;
-            Rec r{kind, phase, nullptr, nullptr};
+        const int ph = phase_of(h, rs.step_base);
+        for (int k = 0; k < kClasses && rc == PC_OK; ++k) {
+            const int cls = (h->l0_class + k) % kClasses;
+            const int n = h->cnt[cls][ph];
+            if (n <= 0) continue;
+            Rec r{cls, ph, nullptr, nullptr};
             cudaEventCreate(&r.a);
             cudaEventCreate(&r.b);
             cudaEventRecord(r.a, h->stream);
-            cudaError_t e = kind < 3 ? launch_fire(kind, grid, h->fire_maxN[kind], h->bank, h->d_fire[kind],
-                                                   h->d_fire_off[kind], rs, nullptr, 0, h->stream)
-                                     : launch_spread(grid, h->bank, h->d_spread, h->d_spread_off, rs, nullptr, 0,
-                                                     h->stream);
+            cudaError_t e = launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs,
+                                              nullptr, 0, h->stream);
             cudaEventRecord(r.b, h->stream);
             recs.push_back(r);
             h->launches += 1;
@@ -961,15 +1061,14 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     }
     h->frame_num += nsteps;
     cudaError_t se = cudaStreamSynchronize(h->stream);
-    double ms[4] = {0, 0, 0, 0}, bytes[4] = {0, 0, 0, 0};
-    long long cnt[4] = {0, 0, 0, 0};
+    double ms[kClasses] = {0, 0, 0}, bytes[kClasses] = {0, 0, 0};
+    long long cnt[kClasses] = {0, 0, 0};
     for (auto& r : recs) {
         float t = 0.f;
-        const double b = r.kind < 3 ? h->fire_bytes[r.kind][r.phase] : h->spread_bytes[r.phase];
-        if (se == cudaSuccess && b > 0 && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
-            ms[r.kind] += t;
-            bytes[r.kind] += b;
-            cnt[r.kind] += 1;
+        if (se == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+            ms[r.cls] += t;
+            bytes[r.cls] += h->alg_bytes[r.cls][r.phase];
+            cnt[r.cls] += 1;
         }
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -977,12 +1076,13 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     if (rc) return rc;
     if (se != cudaSuccess) return cuda_fail(h, se, "profile sync");
     int n = 0;
-    for (int kind = 0; kind < 4 && n < max_kinds; ++kind) {
-        if (cnt[kind] == 0) continue;
-        std::snprintf(out[n].name, sizeof out[n].name, "%s", names[kind]);
-        out[n].launches = cnt[kind];
-        out[n].total_ms = ms[kind];
-        out[n].alg_bytes = bytes[kind];
+    for (int k = 0; k < kClasses && n < max_kinds; ++k) {
+        const int cls = (h->l0_class + k) % kClasses;
+        if (cnt[cls] == 0) continue;
+        std::snprintf(out[n].name, sizeof out[n].name, "%s", names[cls]);
+        out[n].launches = cnt[cls];
+        out[n].total_ms = ms[cls];
+        out[n].alg_bytes = bytes[cls];
         ++n;
     }
     if (n_kinds) *n_kinds = n;

@@ -5,30 +5,22 @@
 //   per PC:    input ring xring[Rin]           (time domain, Rin = pow2 >= 2 N_max)
 //   per level: H[P][cs]  filter spectra        (float2, cs = N + 2 row stride)
 //              X[P][cs]  input-spectrum ring   (slot b mod P holds block b)
-//              Yp[cs]    partial sum over parts p >= 1 for the next block
+//              Yp[2][cs] partial sums of the FDL MAC for the next block
 //              yring[R]  output ring            (levels >= 1; R = pow2 >= s_L + N0)
 //   per PC:    pcout[N0] level sum (only when an output mixes several PCs)
 //   global:    twiddle table W[2^wlog], per-phase task tables, mix counters.
 // Rows are (N + 2) complex values so every row starts 16-byte aligned and
 // the MAC can move two bins per float4.
 #pragma once
-#include <cstdint>
-
-#ifdef __CUDACC__
 #include <cuda_runtime.h>
-#else
-struct float2_ { float x, y; };
-#endif
+
+#include <cstdint>
 
 namespace pcg {
 
-#ifdef __CUDACC__
-using cfloat2 = float2;
-#else
-using cfloat2 = float2_;
-#endif
+constexpr int kEmitLevels = 4;   // level-0 tasks carry the output rings of up to 4 more levels
 
-// One partition level of one PC.
+// One partition level of one PC (host copy and device table).
 struct DevLevel {
     int N;          // block size N_L
     int logN;       // log2 N_L
@@ -38,9 +30,9 @@ struct DevLevel {
     int cs;         // row stride in complex values (N_L + 2)
     int rmask;      // output ring size - 1 (levels >= 1)
     int pc;         // owning PC
-    cfloat2* H;     // [P][cs]
-    cfloat2* X;     // [P][cs]
-    cfloat2* Yp;    // [cs]
+    float2* H;      // [P][cs]
+    float2* X;      // [P][cs]
+    float2* Yp;     // [2][cs]
     float* yring;   // [rmask + 1]
 };
 
@@ -60,6 +52,28 @@ struct DevPC {
     float* pcout;    // [N0] (mix_mode 2)
 };
 
+// A unit of work of one base step, self-contained so a CTA needs one load
+// to start.  kind 0 (fire): compute one level block -- window, FFT, MAC,
+// inverse FFT, output (level 0 also emits the step's output).  kind 1
+// (spread): partial FDL MAC over bins [k0, k1) for a level's next block.
+struct Task {
+    int kind, N, logN, P;
+    int T, s_blocks, cs, rmask;
+    int k0, k1, M, in_ch;
+    int out_ch, mix_mode, zero_outs, zero_off;
+    int rin_mask, lv_index, p_lo, pad0;   // p_lo: first part summed by a spread task
+    float scale, pad1, pad2, pad3;
+    float2* H;
+    float2* X;
+    float2* Yp;
+    float* yring;
+    float* xring;
+    float* pcout;
+    float* eyring[kEmitLevels];   // level-0 fire: output rings of levels 1..4
+    int emask[kEmitLevels];
+};
+static_assert(sizeof(Task) == 192, "Task record is loaded as 12 x 16 bytes");
+
 // Where step c's input/output live: base + (c - step0) * step_stride +
 // sample * sample_stride + channel * ch_stride.
 struct IOView {
@@ -72,30 +86,20 @@ struct IOView {
 
 // Per-run state read by every step kernel.
 struct RunState {
-    long long step_base;   // global step of the first launch in this batch
+    long long step_base;   // global step of step_in_batch == 0
     IOView io;
 };
-
-// A fire task: compute one level block (FFT -> MAC -> IFFT) of one level.
-struct FireTask {
-    int level;   // index into the level array
-};
-
-// A spread task: partial MAC over parts p >= 1 for bins [k0, k1).
-struct SpreadTask {
-    int level;
-    int k0, k1;
-};
+static_assert(sizeof(RunState) == 80, "RunState is loaded as 5 x 16 bytes");
 
 // Static tables the step kernels read.
 struct Bank {
     const DevPC* pcs;
     const DevLevel* lv;
-    const cfloat2* W;      // twiddles, 2^wlog entries
+    const float2* W;       // twiddles, 2^wlog entries
     int wlog;
     int N0;
-    int H;                 // hyperperiod in steps (power of two)
     int n_out;
+    int pad;
     // per output channel mixing lists (mix_mode 2): out_off[o]..out_off[o+1]
     const int* out_off;
     const int* out_pcs;

@@ -15,8 +15,10 @@
 // stage stages its butterflies' inputs in registers, so one N-element
 // shared buffer suffices (a barrier separates the reads from the writes).
 //
-// Twiddles come from a table W[m] = exp(-2 pi i m / 2^wlog) computed in
-// double on the host and rounded once to float.
+// Twiddles come from a quarter-wave table in shared memory,
+// tw[m] = exp(-2 pi i m / 2N) for 0 <= m < N/2, filled once per CTA from a
+// global table computed in double on the host; other angles follow by
+// quarter-turn symmetry.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -29,16 +31,39 @@ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 
-// twiddle for a full turn split into 2^lg parts, index m (m < 2^lg)
-__device__ __forceinline__ float2 twiddle(const float2* __restrict__ W, int wlog, int m, int lg, bool inv) {
-    float2 w = __ldg(&W[m << (wlog - lg)]);
-    return inv ? cconj(w) : w;
+// Quarter-wave twiddle table of a 2N-point circle in shared memory.
+struct Twiddles {
+    const float2* tab;   // N/2 entries
+    int logN;            // log2 N
+
+    // exp(-+2 pi i a / 2^lg), 0 <= a < 2^lg, 2^lg <= 2N
+    __device__ __forceinline__ float2 get(int a, int lg, bool inv) const {
+        const int a2 = a << (logN + 1 - lg);           // index on the 2N circle
+        const int q = a2 >> (logN - 1);                // quadrant
+        const float2 t = tab[a2 & ((1 << (logN - 1)) - 1)];
+        float2 w;
+        switch (q & 3) {
+            case 0: w = t; break;
+            case 1: w = make_float2(t.y, -t.x); break;   // * (-i)
+            case 2: w = make_float2(-t.x, -t.y); break;
+            default: w = make_float2(-t.y, t.x); break;  // * (+i)
+        }
+        return inv ? cconj(w) : w;
+    }
+};
+
+// Fill the quarter-wave table for an N-point complex FFT (2N-point real
+// transform) from the global table W of 2^wlog entries (2^wlog >= 2N).
+template <int NT>
+__device__ __forceinline__ void load_twiddles(float2* tab, int logN, const float2* __restrict__ W, int wlog) {
+    const int n = 1 << (logN - 1);   // angles [0, pi/2): get() never needs index N/2
+    const int sh = wlog - (logN + 1);
+    for (int m = threadIdx.x; m < n; m += NT) tab[m] = __ldg(&W[m << sh]);
 }
 
 // One radix-4 Stockham stage (Ns = product of previous radices).
 template <int NT, int MAXB>
-__device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, const float2* __restrict__ W,
-                                         int wlog, bool inv) {
+__device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, const Twiddles& tw, bool inv) {
     const int nb = N >> 2;
     float2 v[MAXB][4];
 #pragma unroll
@@ -57,9 +82,9 @@ __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, con
             const int k = j & (Ns - 1);
             if (Ns > 1) {
                 const int lg = lgNs + 2;
-                v[i][1] = cmul(v[i][1], twiddle(W, wlog, k, lg, inv));
-                v[i][2] = cmul(v[i][2], twiddle(W, wlog, 2 * k, lg, inv));
-                v[i][3] = cmul(v[i][3], twiddle(W, wlog, 3 * k, lg, inv));
+                v[i][1] = cmul(v[i][1], tw.get(k, lg, inv));
+                v[i][2] = cmul(v[i][2], tw.get(2 * k, lg, inv));
+                v[i][3] = cmul(v[i][3], tw.get(3 * k, lg, inv));
             }
             const float2 a0 = cadd(v[i][0], v[i][2]);
             const float2 a1 = csub(v[i][0], v[i][2]);
@@ -79,8 +104,7 @@ __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, con
 
 // Final radix-2 Stockham stage.
 template <int NT, int MAXB>
-__device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, const float2* __restrict__ W,
-                                         int wlog, bool inv) {
+__device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, const Twiddles& tw, bool inv) {
     const int nb = N >> 1;
     float2 v[2 * MAXB][2];
 #pragma unroll
@@ -98,7 +122,7 @@ __device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, con
         if (j < nb) {
             const int k = j & (Ns - 1);
             float2 b = v[i][1];
-            if (Ns > 1) b = cmul(b, twiddle(W, wlog, k, lgNs + 1, inv));
+            if (Ns > 1) b = cmul(b, tw.get(k, lgNs + 1, inv));
             const int base = ((j - k) << 1) + k;
             s[base] = cadd(v[i][0], b);
             s[base + Ns] = csub(v[i][0], b);
@@ -108,19 +132,19 @@ __device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, con
 }
 
 // In-place complex FFT of N = 2^logN points in shared memory (unnormalised).
-// Requires N / 4 <= NT * MAXB.  Callers must __syncthreads() before (data
-// written) -- the function ends with a barrier.
+// Requires N / 4 <= NT * MAXB and 16 <= N.  Callers __syncthreads() after
+// writing the data; the function ends with a barrier.
 template <int NT, int MAXB>
-__device__ void fft_smem(float2* s, int N, int logN, const float2* __restrict__ W, int wlog, bool inv) {
+__device__ void fft_smem(float2* s, int N, int logN, const Twiddles& tw, bool inv) {
     int Ns = 1, lgNs = 0;
-    for (; lgNs + 2 <= logN; lgNs += 2, Ns <<= 2) stage_r4<NT, MAXB>(s, N, Ns, lgNs, W, wlog, inv);
-    if (lgNs < logN) stage_r2<NT, MAXB>(s, N, Ns, lgNs, W, wlog, inv);
+    for (; lgNs + 2 <= logN; lgNs += 2, Ns <<= 2) stage_r4<NT, MAXB>(s, N, Ns, lgNs, tw, inv);
+    if (lgNs < logN) stage_r2<NT, MAXB>(s, N, Ns, lgNs, tw, inv);
 }
 
 // Split post-pass for the pair (k, N-k), 0 <= k <= N/2, on Z = FFT_N(z).
 // Returns X[k] in xk and X[N-k] in xnk (for k == 0: X[0] and X[N]).
-__device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int N, int logN,
-                                           const float2* __restrict__ W, int wlog, float2& xk, float2& xnk) {
+__device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int logN, const Twiddles& tw, float2& xk,
+                                           float2& xnk) {
     if (k == 0) {
         xk = make_float2(zk.x + zk.y, 0.0f);
         xnk = make_float2(zk.x - zk.y, 0.0f);
@@ -128,7 +152,7 @@ __device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int N, 
     }
     const float2 E = make_float2(0.5f * (zk.x + znk.x), 0.5f * (zk.y - znk.y));
     const float2 O = make_float2(0.5f * (zk.y + znk.y), -0.5f * (zk.x - znk.x));
-    const float2 w = twiddle(W, wlog, k, logN + 1, false);   // e^{-i pi k / N}
+    const float2 w = tw.get(k, logN + 1, false);   // e^{-i pi k / N}
     const float2 wO = cmul(w, O);
     xk = cadd(E, wO);
     xnk = cconj(csub(E, wO));
@@ -137,15 +161,15 @@ __device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int N, 
 // Inverse pre-pass for the pair (k, N-k) from Y[k] (yk) and Y[N-k] (ynk);
 // for k == 0 yk = Y[0], ynk = Y[N] and only zk (= Z'[0]) is meaningful.
 // Imaginary parts of Y[0] and Y[N] are ignored, as FFTW's c2r does.
-__device__ __forceinline__ void irfft_merge(float2 yk, float2 ynk, int k, int N, int logN,
-                                            const float2* __restrict__ W, int wlog, float2& zk, float2& znk) {
+__device__ __forceinline__ void irfft_merge(float2 yk, float2 ynk, int k, int logN, const Twiddles& tw, float2& zk,
+                                            float2& znk) {
     if (k == 0) {
         yk.y = 0.0f;
         ynk.y = 0.0f;
     }
     const float2 A = make_float2(yk.x + ynk.x, yk.y - ynk.y);   // Y[k] + conj(Y[N-k])
     const float2 B = make_float2(yk.x - ynk.x, yk.y + ynk.y);   // Y[k] - conj(Y[N-k])
-    const float2 w = twiddle(W, wlog, k, logN + 1, false);
+    const float2 w = tw.get(k, logN + 1, false);
     const float2 cB = cmul(cconj(w), B);                          // conj(w^k) B
     zk = make_float2(A.x - cB.y, A.y + cB.x);                     // A + i conj(w^k) B
     const float2 wcB = cmul(w, cconj(B));                         // w^k conj(B)

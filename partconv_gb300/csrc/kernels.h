@@ -2,12 +2,11 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include "engine_types.h"
 
 namespace pcg {
-
-// threads per spread CTA; a spread task covers at most 2 * kSpreadNT bins
-constexpr int kSpreadNT = 256;
 
 // one filter-spectrum row: dst[0..N] = rfft([0_N, src[0..len)]) / 2N
 struct SpectraJob {
@@ -18,15 +17,15 @@ struct SpectraJob {
     float2* dst;
 };
 
-// fire kernel class by block size: 0 (N <= 1024), 1 (N <= 4096), 2 (N <= 16384)
+// kernel class by block size: 0 (N <= 1024), 1 (N <= 4096), 2 (N <= 16384)
 int fire_class_of(int N);
-int fire_threads(int cls);
+// threads per CTA of a class; a spread task covers 2 * threads bins
+int class_threads(int cls);
+size_t class_smem_bytes(int cls, int maxN);
 
 cudaError_t prepare_kernels();
-cudaError_t launch_fire(int cls, int grid, int maxN, const Bank& bank, const FireTask* tasks, const int* off,
-                        const RunState& rs, const RunState* rs_dev, int step_in_batch, cudaStream_t st);
-cudaError_t launch_spread(int grid, const Bank& bank, const SpreadTask* tasks, const int* off, const RunState& rs,
-                          const RunState* rs_dev, int step_in_batch, cudaStream_t st);
+cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
+                              const RunState* rs_dev, int step_in_batch, cudaStream_t st);
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,
                            cudaStream_t st);
 cudaError_t launch_set_state(RunState* dst, const RunState& v, cudaStream_t st);

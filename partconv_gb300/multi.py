@@ -165,14 +165,18 @@ class PartConvMulti:
 
     def process_device(self, d_out, d_in, frames: int, layout: int = nat.PC_INTERLEAVED, stream=None) -> int:
         """Device buffers (torch tensors or integer device pointers) on a
-        CUDA stream (torch stream, raw handle int, or None for the handle's
-        own stream).  Enqueues only; the caller synchronises."""
+        CUDA stream (torch stream, raw handle int; None means torch's current
+        stream).  Enqueues only; the caller synchronises."""
         po = d_out.data_ptr() if hasattr(d_out, "data_ptr") else int(d_out)
         pi = d_in.data_ptr() if hasattr(d_in, "data_ptr") else int(d_in)
-        if stream is not None and hasattr(stream, "cuda_stream"):
+        if stream is None:
+            import torch
+
+            stream = torch.cuda.current_stream()
+        if hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
         nat.check(self._h, self._lib.pc_process_device(self._h, C.c_void_p(po), C.c_void_p(pi), int(frames),
-                                                       int(layout), C.c_void_p(stream) if stream else None))
+                                                       int(layout), C.c_void_p(int(stream))))
         self._frame_num += frames // self.buffer_size
         return 0
 

@@ -412,7 +412,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     // Tasks point into the arena, so they are built after the state offsets
     // are known; first count them to size the table.
     std::vector<std::vector<std::vector<Task>>> lists(kClasses, std::vector<std::vector<Task>>(Hh));
-    auto spread_bins = [&](int cls) { return 2 * class_threads(cls); };
     for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(Hh, 0.0);
     // order: larger fires first (longest CTAs start first), then level-0
     // fires, then spread tasks
@@ -476,7 +475,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
                 p_lo = 1;
             }
-            for (int k0 = lo; k0 < hi; k0 += spread_bins(sc)) {
+            for (int k0 = lo; k0 < hi; k0 += spread_task_bins()) {
                 Task t{};
                 t.kind = 1;
                 t.N = l.N;
@@ -485,7 +484,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 t.s_blocks = l.s_blocks;
                 t.cs = l.cs;
                 t.k0 = k0;
-                t.k1 = std::min(hi, k0 + spread_bins(sc));
+                t.k1 = std::min(hi, k0 + spread_task_bins());
                 t.p_lo = p_lo;
                 t.lv_index = li;
                 lists[sc][g].push_back(t);

@@ -19,8 +19,10 @@ struct SpectraJob {
 
 // kernel class by block size: 0 (N <= 1024), 1 (N <= 4096), 2 (N <= 16384)
 int fire_class_of(int N);
-// threads per CTA of a class; a spread task covers 2 * threads bins
+// threads per CTA of a class
 int class_threads(int cls);
+// bins one spread task covers
+int spread_task_bins();
 size_t class_smem_bytes(int cls, int maxN);
 
 cudaError_t prepare_kernels();

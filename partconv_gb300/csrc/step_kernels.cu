@@ -24,6 +24,10 @@
 // Tasks of one step touch disjoint data (level 0's partial sums are double
 // buffered by block parity), so every CTA of a step runs independently; the
 // next step depends on this one.
+//
+// Latency: a small fire is a chain of dependent steps, so every phase that
+// touches global memory first issues all of its loads into registers and
+// only then uses them (one memory round trip per phase).
 #include <cuda_runtime.h>
 
 #include "engine_types.h"
@@ -37,18 +41,57 @@ __device__ __forceinline__ long long imod(long long a, long long m) {
     return r < 0 ? r + m : r;
 }
 
+__device__ __forceinline__ float4 f4mac(float4 acc, float4 x, float4 h) {
+    // two complex multiply-adds: (x.x + i x.y)(h.x + i h.y), (x.z + i x.w)(h.z + i h.w)
+    acc.x += x.x * h.x - x.y * h.y;
+    acc.y += x.x * h.y + x.y * h.x;
+    acc.z += x.z * h.z - x.w * h.w;
+    acc.w += x.z * h.w + x.w * h.z;
+    return acc;
+}
+__device__ __forceinline__ float4 f4mul(float4 x, float4 h) { return f4mac(make_float4(0.f, 0.f, 0.f, 0.f), x, h); }
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// Kernel class: threads per CTA, largest block size, operand prefetch.
+template <int NT_, int MAXN_, bool PREFETCH_>
+struct Cls {
+    static constexpr int NT = NT_;
+    static constexpr int MAXN = MAXN_;
+    static constexpr bool PREFETCH = PREFETCH_;
+    static constexpr int MAXB = MAXN / 4 / NT;                   // radix-4 butterflies per thread
+    static constexpr int MAXQ = (MAXN / 2 + NT - 1) / NT;        // window quads (4 samples) per thread
+    static constexpr int MAXT = (MAXN / 2 + NT - 1) / NT;        // twiddles per thread
+    static constexpr int MAXK = (MAXN / 2 + 1 + NT - 1) / NT;    // bin pairs per thread (prefetch)
+    static constexpr int MAXE = (MAXN / 4 + NT - 1) / NT;        // output quads per thread
+    static constexpr int SPLIT_CH = 4;                           // post-FFT pairs loaded per batch
+    static_assert(MAXB >= 1, "class too small");
+};
+using Cls0 = Cls<256, 1024, true>;
+using Cls1 = Cls<512, 4096, false>;
+using Cls2 = Cls<1024, 16384, false>;
+
 // dynamic shared memory bytes of a fire for block size N
 __host__ __device__ constexpr size_t fire_smem_bytes(int N, bool prefetch) {
-    // data N + quarter twiddles N/2 (+ yacc N+2, h0 N+2, emit N floats)
+    // data N + quarter twiddles N/2 complex (+ yacc N+2, h0 N+2 complex, emit N floats)
     return prefetch ? (size_t)8 * N + 4 * N + 16 * ((size_t)N + 2) + 4 * (size_t)N
                     : (size_t)8 * N + 4 * (size_t)N;
 }
 
 // ---------------------------------------------------------------------------
+// Spread: NT threads = G part-groups x 64 threads; a thread owns two bins,
+// group g sums parts p_lo + g, p_lo + g + G, ...; groups are added in order.
+// ---------------------------------------------------------------------------
+constexpr int kSpreadLanes = 64;   // threads per part-group: a task covers 128 bins
+
 template <int NT>
-__device__ __forceinline__ void spread_body(const Task& tk, long long c) {
-    const int k = tk.k0 + 2 * threadIdx.x;
-    if (k >= tk.k1) return;
+__device__ __forceinline__ void spread_body(const Task& tk, long long c, float4* red) {
+    constexpr int G = NT / kSpreadLanes;
+    const int lane = threadIdx.x % kSpreadLanes;
+    const int g = threadIdx.x / kSpreadLanes;
+    const int k = tk.k0 + 2 * lane;
+    const bool active = k < tk.k1;
     long long bt;      // block whose partial sum this step builds
     float2* dst;
     if (tk.T == 1) {   // level 0: parts p >= 2 of block c + 1
@@ -59,28 +102,46 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c) {
         dst = tk.Yp;
     }
     const int P = tk.P;
-    const int rs4 = tk.cs >> 1;   // row stride in float4
+    const size_t rs4 = (size_t)(tk.cs >> 1);   // row stride in float4
     const float4* X4 = reinterpret_cast<const float4*>(tk.X + k);
     const float4* H4 = reinterpret_cast<const float4*>(tk.H + k);
-    int sl = (int)imod(bt - tk.p_lo, P);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 4
-    for (int p = tk.p_lo; p < P; ++p) {
-        const float4 x = __ldcg(X4 + (size_t)sl * rs4);
-        const float4 h = __ldg(H4 + (size_t)p * rs4);
-        acc.x += x.x * h.x - x.y * h.y;
-        acc.y += x.x * h.y + x.y * h.x;
-        acc.z += x.z * h.z - x.w * h.w;
-        acc.w += x.z * h.w + x.w * h.z;
-        sl = (sl == 0) ? P - 1 : sl - 1;
+    if (active) {
+        constexpr int U = 4;   // parts whose loads are in flight together
+        for (int p0 = tk.p_lo + g; p0 < P; p0 += U * G) {
+            float4 xv[U], hv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int p = p0 + u * G;
+                if (p < P) {
+                    const int sl = (int)imod(bt - p, P);
+                    xv[u] = __ldcg(X4 + (size_t)sl * rs4);
+                    hv[u] = __ldg(H4 + (size_t)p * rs4);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (p0 + u * G < P) acc = f4mac(acc, xv[u], hv[u]);
+        }
     }
-    *reinterpret_cast<float4*>(dst + k) = acc;
+    if (G > 1) {
+        if (g > 0) red[(g - 1) * kSpreadLanes + lane] = acc;
+        __syncthreads();
+        if (g == 0 && active) {
+#pragma unroll
+            for (int j = 1; j < G; ++j) acc = f4add(acc, red[(j - 1) * kSpreadLanes + lane]);
+            *reinterpret_cast<float4*>(dst + k) = acc;
+        }
+    } else if (active) {
+        *reinterpret_cast<float4*>(dst + k) = acc;
+    }
 }
 
 // ---------------------------------------------------------------------------
-template <int NT, int MAXB, bool PREFETCH>
+template <class C>
 __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, const RunState& rs, long long c,
                                           float2* smem, int* s_last) {
+    constexpr int NT = C::NT;
     const int tid = threadIdx.x;
     const int N = tk.N, logN = tk.logN, P = tk.P, cs = tk.cs;
     const int N0 = bank.N0;
@@ -101,108 +162,180 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const float* in = rs.io.in + io_step * rs.io.in_step + (long long)tk.in_ch * rs.io.in_ch;
     const long long isamp = rs.io.in_sample;
     const float scale = tk.scale;
-
-    // ---- prologue: window, twiddles, MAC operands, emission slices ------------
-    for (int n = tid; n < N; n += NT) {
-        const long long ta = t_end - 2LL * N + 2LL * n;
-        float a, bb;
-        if (ta >= t_new) {
-            const long long i = ta - t_new;
-            a = in[i * isamp] * scale;
-            bb = in[(i + 1) * isamp] * scale;
-            if (l0) {   // level 0 appends this step's input to the PC's ring
-                tk.xring[ta & tk.rin_mask] = a;
-                tk.xring[(ta + 1) & tk.rin_mask] = bb;
-            }
-        } else {
-            a = __ldcg(&tk.xring[ta & tk.rin_mask]);
-            bb = __ldcg(&tk.xring[(ta + 1) & tk.rin_mask]);
-        }
-        s[n] = make_float2(a, bb);
-    }
-    load_twiddles<NT>(twt, logN, bank.W, bank.wlog);
     const float2* X1 = tk.X + (size_t)imod(b - 1, P) * cs;   // block b-1 (level 0, p = 1)
     const float2* Ypb = tk.Yp + (l0 ? (size_t)(b & 1) * cs : 0);
-    if (PREFETCH) {
-        for (int k = tid; k <= N; k += NT) {
-            float2 acc = make_float2(0.f, 0.f);
-            if (l0) {
-                if (P >= 2) acc = cmul(__ldcg(&X1[k]), __ldg(&tk.H[cs + k]));
-                if (P >= 3) acc = cadd(acc, __ldcg(&Ypb[k]));
-            } else if (P >= 2) {
-                acc = __ldcg(&Ypb[k]);
-            }
-            yacc[k] = acc;
-            h0s[k] = __ldg(&tk.H[k]);
-        }
-        if (l0 && tk.M > 1) {
-            for (int i = tid; i < N0; i += NT) {
-                float v = 0.f;
-                const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
-                for (int L = 0; L < Le; ++L) v += __ldcg(&tk.eyring[L][(t_new + i) & tk.emask[L]]);
-                for (int L = kEmitLevels + 1; L < tk.M; ++L) {
-                    const DevLevel& l2 = bank.lv[tk.lv_index + L];
-                    v += __ldcg(&l2.yring[(t_new + i) & l2.rmask]);
+
+    // ---- prologue: issue every load, then store -------------------------------------
+    {
+        const int nq = N >> 1;        // window quads: samples t_end - 2N + 4q .. + 3
+        float4 wv[C::MAXQ];
+#pragma unroll
+        for (int i = 0; i < C::MAXQ; ++i) {
+            const int qd = tid + i * NT;
+            if (qd < nq) {
+                const long long ta = t_end - 2LL * N + 4LL * qd;
+                if (ta >= t_new) {
+                    const long long j = ta - t_new;
+                    wv[i] = make_float4(in[j * isamp] * scale, in[(j + 1) * isamp] * scale,
+                                        in[(j + 2) * isamp] * scale, in[(j + 3) * isamp] * scale);
+                } else {
+                    wv[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
                 }
-                emit[i] = v;
+            }
+        }
+        const int ntw = N >> 1;
+        const int sh = bank.wlog - (logN + 1);
+        float2 tv[C::MAXT];
+#pragma unroll
+        for (int i = 0; i < C::MAXT; ++i) {
+            const int m = tid + i * NT;
+            if (m < ntw) tv[i] = __ldg(&bank.W[m << sh]);
+        }
+        float4 xa[C::PREFETCH ? C::MAXK : 1], ha[C::PREFETCH ? C::MAXK : 1], ya[C::PREFETCH ? C::MAXK : 1],
+            h0a[C::PREFETCH ? C::MAXK : 1];
+        float4 ev[C::PREFETCH ? C::MAXE : 1];
+        const int npair = (N + 2) >> 1;
+        if (C::PREFETCH) {
+#pragma unroll
+            for (int i = 0; i < C::MAXK; ++i) {
+                const int kk = 2 * (tid + i * NT);
+                if (kk < 2 * npair) {
+                    h0a[i] = __ldg(reinterpret_cast<const float4*>(tk.H + kk));
+                    if (l0 && P >= 2) {
+                        xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
+                        ha[i] = __ldg(reinterpret_cast<const float4*>(tk.H + cs + kk));
+                    }
+                    if ((l0 && P >= 3) || (!l0 && P >= 2)) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
+                }
+            }
+            if (l0) {
+                const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
+#pragma unroll
+                for (int i = 0; i < C::MAXE; ++i) {
+                    const int e4 = tid + i * NT;
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (4 * e4 < N0) {
+                        for (int L = 0; L < Le; ++L)
+                            v = f4add(v, __ldcg(reinterpret_cast<const float4*>(
+                                             tk.eyring[L] + ((t_new + 4 * e4) & tk.emask[L]))));
+                    }
+                    ev[i] = v;
+                }
+            }
+        }
+        // stores
+#pragma unroll
+        for (int i = 0; i < C::MAXQ; ++i) {
+            const int qd = tid + i * NT;
+            if (qd < nq) {
+                s[2 * qd] = make_float2(wv[i].x, wv[i].y);
+                s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
+                const long long ta = t_end - 2LL * N + 4LL * qd;
+                if (l0 && ta >= t_new)   // level 0 appends this step's input to the PC's ring
+                    *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < C::MAXT; ++i) {
+            const int m = tid + i * NT;
+            if (m < ntw) twt[m] = tv[i];
+        }
+        if (C::PREFETCH) {
+#pragma unroll
+            for (int i = 0; i < C::MAXK; ++i) {
+                const int kk = 2 * (tid + i * NT);
+                if (kk < 2 * npair) {
+                    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (l0 && P >= 2) acc = f4mul(xa[i], ha[i]);
+                    if ((l0 && P >= 3) || (!l0 && P >= 2)) acc = f4add(acc, ya[i]);
+                    *reinterpret_cast<float4*>(yacc + kk) = acc;
+                    *reinterpret_cast<float4*>(h0s + kk) = h0a[i];
+                }
+            }
+            if (l0) {
+                for (int L = kEmitLevels + 1; L < tk.M; ++L) {   // rare: more than 5 levels
+                    const DevLevel& l2 = bank.lv[tk.lv_index + L];
+#pragma unroll
+                    for (int i = 0; i < C::MAXE; ++i) {
+                        const int e4 = tid + i * NT;
+                        if (4 * e4 < N0)
+                            ev[i] = f4add(ev[i], __ldcg(reinterpret_cast<const float4*>(
+                                                     l2.yring + ((t_new + 4 * e4) & l2.rmask))));
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < C::MAXE; ++i) {
+                    const int e4 = tid + i * NT;
+                    if (4 * e4 < N0) *reinterpret_cast<float4*>(emit + 4 * e4) = ev[i];
+                }
             }
         }
     }
     __syncthreads();
 
-    fft_smem<NT, MAXB>(s, N, logN, tw, false);
+    fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
 
     // ---- split, FDL MAC, inverse merge -------------------------------------------
     float2* __restrict__ Xs = tk.X + (size_t)slot * cs;
     const int half = N >> 1;
-    for (int k = tid; k <= half; k += NT) {
+    auto finish_pair = [&](int k, float2 h0k, float2 h0nk, float2 ak, float2 ank) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
         rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
         const int bk = k, bnk = N - k;   // k == 0 pairs bin 0 with bin N
         Xs[bk] = xk;
         if (bnk != bk) Xs[bnk] = xnk;
-        float2 h0k, h0nk, ak, ank;
-        if (PREFETCH) {
-            h0k = h0s[bk];
-            h0nk = h0s[bnk];
-            ak = yacc[bk];
-            ank = yacc[bnk];
-        } else {
-            h0k = __ldg(&tk.H[bk]);
-            h0nk = __ldg(&tk.H[bnk]);
-            ak = make_float2(0.f, 0.f);
-            ank = ak;
-            if (l0) {
-                if (P >= 2) {
-                    ak = cmul(__ldcg(&X1[bk]), __ldg(&tk.H[cs + bk]));
-                    ank = cmul(__ldcg(&X1[bnk]), __ldg(&tk.H[cs + bnk]));
-                }
-                if (P >= 3) {
-                    ak = cadd(ak, __ldcg(&Ypb[bk]));
-                    ank = cadd(ank, __ldcg(&Ypb[bnk]));
-                }
-            } else if (P >= 2) {
-                ak = __ldcg(&Ypb[bk]);
-                ank = __ldcg(&Ypb[bnk]);
-            }
-        }
         const float2 yk = cadd(cmul(xk, h0k), ak);
         const float2 ynk = cadd(cmul(xnk, h0nk), ank);
         float2 zk, znk;
         irfft_merge(yk, ynk, k, logN, tw, zk, znk);
         s[k] = zk;
         if (k != 0 && k != half) s[N - k] = znk;
+    };
+    if (C::PREFETCH) {
+        for (int k = tid; k <= half; k += NT) finish_pair(k, h0s[k], h0s[N - k], yacc[k], yacc[N - k]);
+    } else {
+        constexpr int CH = C::SPLIT_CH;
+        const bool usey = (l0 && P >= 3) || (!l0 && P >= 2);
+        for (int k0 = tid; k0 <= half; k0 += CH * NT) {
+            float2 h0v[CH][2], av[CH][2];
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const int k = k0 + u * NT;
+                if (k <= half) {
+                    const int bnk = N - k;
+                    h0v[u][0] = __ldg(&tk.H[k]);
+                    h0v[u][1] = __ldg(&tk.H[bnk]);
+                    av[u][0] = make_float2(0.f, 0.f);
+                    av[u][1] = av[u][0];
+                    if (usey) {
+                        av[u][0] = __ldcg(&Ypb[k]);
+                        av[u][1] = __ldcg(&Ypb[bnk]);
+                    }
+                    if (l0 && P >= 2) {
+                        av[u][0] = cadd(av[u][0], cmul(__ldcg(&X1[k]), __ldg(&tk.H[cs + k])));
+                        av[u][1] = cadd(av[u][1], cmul(__ldcg(&X1[bnk]), __ldg(&tk.H[cs + bnk])));
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const int k = k0 + u * NT;
+                if (k <= half) finish_pair(k, h0v[u][0], h0v[u][1], av[u][0], av[u][1]);
+            }
+        }
     }
     __syncthreads();
 
-    fft_smem<NT, MAXB>(s, N, logN, tw, true);
+    fft_smem<NT, C::MAXB>(s, N, logN, tw, true);
 
     const float* sf = reinterpret_cast<const float*>(s);   // y[i] = sf[i], i < 2N
     if (!l0) {
         // level block b covers output samples [b N, (b+1) N)
         const long long t0 = b * (long long)N;
-        for (int i = tid; i < N; i += NT) tk.yring[(t0 + i) & tk.rmask] = sf[i];
+        for (int i4 = tid; 4 * i4 < N; i4 += NT)
+            *reinterpret_cast<float4*>(tk.yring + ((t0 + 4 * i4) & tk.rmask)) =
+                reinterpret_cast<const float4*>(sf)[i4];
         return;
     }
 
@@ -211,7 +344,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const long long osamp = rs.io.out_sample, och = rs.io.out_ch;
     for (int i = tid; i < N0; i += NT) {
         float v = sf[i];
-        if (PREFETCH) {
+        if (C::PREFETCH) {
             if (tk.M > 1) v += emit[i];
         } else {
             for (int L = 1; L < tk.M; ++L) {
@@ -251,9 +384,9 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
 // ---------------------------------------------------------------------------
 // The step kernel: CTA i runs task i of this step's task list.
 // ---------------------------------------------------------------------------
-template <int NT, int MAXB, bool PREFETCH>
-__global__ void __launch_bounds__(NT) step_kernel(Bank bank, const Task* __restrict__ tasks, RunState rs_val,
-                                                  const RunState* rs_dev, int step_in_batch) {
+template <class C>
+__global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __restrict__ tasks, RunState rs_val,
+                                                     const RunState* rs_dev, int step_in_batch) {
     extern __shared__ float4 dyn_smem[];
     __shared__ __align__(16) Task tk;
     __shared__ __align__(16) RunState rs;
@@ -263,16 +396,16 @@ __global__ void __launch_bounds__(NT) step_kernel(Bank bank, const Task* __restr
         reinterpret_cast<int4*>(&tk)[tid] = __ldg(reinterpret_cast<const int4*>(tasks + blockIdx.x) + tid);
     } else if (tid >= 32 && tid < 37) {
         const int j = tid - 32;
-        reinterpret_cast<int4*>(&rs)[j] = rs_dev ? __ldcg(reinterpret_cast<const int4*>(rs_dev) + j)
-                                                 : reinterpret_cast<const int4*>(&rs_val)[j];
+        if (rs_dev) reinterpret_cast<int4*>(&rs)[j] = __ldcg(reinterpret_cast<const int4*>(rs_dev) + j);
     }
+    if (!rs_dev && tid == 64) rs = rs_val;
     __syncthreads();
     const long long c = rs.step_base + step_in_batch;
     if (tk.kind == 1) {
-        spread_body<NT>(tk, c);
+        spread_body<C::NT>(tk, c, dyn_smem);
         return;
     }
-    fire_body<NT, MAXB, PREFETCH>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
+    fire_body<C>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
 }
 
 // ---------------------------------------------------------------------------
@@ -317,24 +450,29 @@ __global__ void set_state_kernel(RunState* dst, RunState v) { *dst = v; }
 // ---------------------------------------------------------------------------
 // Host-side launchers.
 // ---------------------------------------------------------------------------
-int fire_class_of(int N) { return N <= 1024 ? 0 : (N <= 4096 ? 1 : 2); }
+int fire_class_of(int N) { return N <= Cls0::MAXN ? 0 : (N <= Cls1::MAXN ? 1 : 2); }
 
-static const int kNT[3] = {128, 256, 512};
-static const bool kPrefetch[3] = {true, true, false};
+static const int kNT[3] = {Cls0::NT, Cls1::NT, Cls2::NT};
+static const bool kPrefetch[3] = {Cls0::PREFETCH, Cls1::PREFETCH, Cls2::PREFETCH};
 int class_threads(int cls) { return kNT[cls]; }
+int spread_task_bins() { return 2 * kSpreadLanes; }
 
-size_t class_smem_bytes(int cls, int maxN) { return fire_smem_bytes(maxN, kPrefetch[cls]); }
+size_t class_smem_bytes(int cls, int maxN) {
+    size_t b = fire_smem_bytes(maxN, kPrefetch[cls]);
+    const size_t red = sizeof(float4) * (size_t)kNT[cls];   // spread part-group partials
+    return b > red ? b : red;
+}
 
 cudaError_t prepare_kernels() {
     cudaError_t e;
-    e = cudaFuncSetAttribute(step_kernel<128, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)fire_smem_bytes(1024, true));
+    e = cudaFuncSetAttribute(step_kernel<Cls0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)class_smem_bytes(0, Cls0::MAXN));
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(step_kernel<256, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)fire_smem_bytes(4096, true));
+    e = cudaFuncSetAttribute(step_kernel<Cls1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)class_smem_bytes(1, Cls1::MAXN));
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(step_kernel<512, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)fire_smem_bytes(16384, false));
+    e = cudaFuncSetAttribute(step_kernel<Cls2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)class_smem_bytes(2, Cls2::MAXN));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(spectra_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(12 * 16384));
@@ -346,9 +484,9 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
     if (grid <= 0) return cudaSuccess;
     const size_t smem = class_smem_bytes(cls, maxN);
     switch (cls) {
-        case 0: step_kernel<128, 2, true><<<grid, 128, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
-        case 1: step_kernel<256, 4, true><<<grid, 256, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
-        default: step_kernel<512, 8, false><<<grid, 512, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
+        case 0: step_kernel<Cls0><<<grid, Cls0::NT, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
+        case 1: step_kernel<Cls1><<<grid, Cls1::NT, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
+        default: step_kernel<Cls2><<<grid, Cls2::NT, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
     }
     return cudaGetLastError();
 }

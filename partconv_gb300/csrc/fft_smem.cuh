@@ -41,13 +41,11 @@ struct Twiddles {
         const int a2 = a << (logN + 1 - lg);           // index on the 2N circle
         const int q = a2 >> (logN - 1);                // quadrant
         const float2 t = tab[a2 & ((1 << (logN - 1)) - 1)];
-        float2 w;
-        switch (q & 3) {
-            case 0: w = t; break;
-            case 1: w = make_float2(t.y, -t.x); break;   // * (-i)
-            case 2: w = make_float2(-t.x, -t.y); break;
-            default: w = make_float2(-t.y, t.x); break;  // * (+i)
-        }
+        // quadrant q rotates by (-i)^q: odd q swaps (x, y) -> (y, -x), q >= 2 negates
+        // (selects rather than a switch, so a warp does not diverge)
+        const bool odd = (q & 1) != 0;
+        const float sg = (q & 2) ? -1.0f : 1.0f;
+        float2 w = make_float2(sg * (odd ? t.y : t.x), sg * (odd ? -t.x : t.y));
         return inv ? cconj(w) : w;
     }
 };

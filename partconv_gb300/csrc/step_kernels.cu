@@ -70,7 +70,7 @@ struct Cls {
 };
 using Cls0 = Cls<256, 1024, true>;
 using Cls1 = Cls<512, 4096, false>;
-using Cls2 = Cls<1024, 16384, false>;
+using Cls2 = Cls<512, 16384, false>;
 
 // dynamic shared memory bytes of a fire for block size N
 __host__ __device__ constexpr size_t fire_smem_bytes(int N, bool prefetch) {
@@ -108,17 +108,22 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
         constexpr int U = 4;   // parts whose loads are in flight together
+        const int Gm = G % P;  // slot step between a group's consecutive parts
+        int sl0 = (int)imod(bt - (tk.p_lo + g), P);   // slot of part p0
         for (int p0 = tk.p_lo + g; p0 < P; p0 += U * G) {
             float4 xv[U], hv[U];
+            int sl = sl0;
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int p = p0 + u * G;
                 if (p < P) {
-                    const int sl = (int)imod(bt - p, P);
                     xv[u] = __ldcg(X4 + (size_t)sl * rs4);
                     hv[u] = __ldg(H4 + (size_t)p * rs4);
                 }
+                sl -= Gm;
+                if (sl < 0) sl += P;
             }
+            sl0 = sl;
 #pragma unroll
             for (int u = 0; u < U; ++u)
                 if (p0 + u * G < P) acc = f4mac(acc, xv[u], hv[u]);
@@ -165,22 +170,23 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const float2* X1 = tk.X + (size_t)imod(b - 1, P) * cs;   // block b-1 (level 0, p = 1)
     const float2* Ypb = tk.Yp + (l0 ? (size_t)(b & 1) * cs : 0);
 
-    // ---- prologue: issue every load, then store -------------------------------------
+    const int nq = N >> 1;                       // window quads: samples t_end - 2N + 4q .. + 3
+    const int nq_old = nq - (N0 >> 2);           // quads before this step's input
+    const int npair = (N + 2) >> 1;              // bin pairs (float4 of two bins)
+    const bool use_x1 = l0 && P >= 2;
+    const bool use_yp = (l0 && P >= 3) || (!l0 && P >= 2);
+
+    // ---- static prologue: nothing earlier steps write (twiddles, filter rows,
+    //      this step's input), so it overlaps the previous step's tail -----------
     {
-        const int nq = N >> 1;        // window quads: samples t_end - 2N + 4q .. + 3
         float4 wv[C::MAXQ];
 #pragma unroll
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
-            if (qd < nq) {
-                const long long ta = t_end - 2LL * N + 4LL * qd;
-                if (ta >= t_new) {
-                    const long long j = ta - t_new;
-                    wv[i] = make_float4(in[j * isamp] * scale, in[(j + 1) * isamp] * scale,
-                                        in[(j + 2) * isamp] * scale, in[(j + 3) * isamp] * scale);
-                } else {
-                    wv[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
-                }
+            if (qd >= nq_old && qd < nq) {
+                const long long j = 4LL * (qd - nq_old);
+                wv[i] = make_float4(in[j * isamp] * scale, in[(j + 1) * isamp] * scale, in[(j + 2) * isamp] * scale,
+                                    in[(j + 3) * isamp] * scale);
             }
         }
         const int ntw = N >> 1;
@@ -191,48 +197,23 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             const int m = tid + i * NT;
             if (m < ntw) tv[i] = __ldg(&bank.W[m << sh]);
         }
-        float4 xa[C::PREFETCH ? C::MAXK : 1], ha[C::PREFETCH ? C::MAXK : 1], ya[C::PREFETCH ? C::MAXK : 1],
-            h0a[C::PREFETCH ? C::MAXK : 1];
-        float4 ev[C::PREFETCH ? C::MAXE : 1];
-        const int npair = (N + 2) >> 1;
+        float4 ha[C::PREFETCH ? C::MAXK : 1], h0a[C::PREFETCH ? C::MAXK : 1];
         if (C::PREFETCH) {
 #pragma unroll
             for (int i = 0; i < C::MAXK; ++i) {
                 const int kk = 2 * (tid + i * NT);
                 if (kk < 2 * npair) {
                     h0a[i] = __ldg(reinterpret_cast<const float4*>(tk.H + kk));
-                    if (l0 && P >= 2) {
-                        xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
-                        ha[i] = __ldg(reinterpret_cast<const float4*>(tk.H + cs + kk));
-                    }
-                    if ((l0 && P >= 3) || (!l0 && P >= 2)) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
-                }
-            }
-            if (l0) {
-                const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
-#pragma unroll
-                for (int i = 0; i < C::MAXE; ++i) {
-                    const int e4 = tid + i * NT;
-                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (4 * e4 < N0) {
-                        for (int L = 0; L < Le; ++L)
-                            v = f4add(v, __ldcg(reinterpret_cast<const float4*>(
-                                             tk.eyring[L] + ((t_new + 4 * e4) & tk.emask[L]))));
-                    }
-                    ev[i] = v;
+                    if (use_x1) ha[i] = __ldg(reinterpret_cast<const float4*>(tk.H + cs + kk));
                 }
             }
         }
-        // stores
 #pragma unroll
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
-            if (qd < nq) {
+            if (qd >= nq_old && qd < nq) {
                 s[2 * qd] = make_float2(wv[i].x, wv[i].y);
                 s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
-                const long long ta = t_end - 2LL * N + 4LL * qd;
-                if (l0 && ta >= t_new)   // level 0 appends this step's input to the PC's ring
-                    *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
             }
         }
 #pragma unroll
@@ -245,28 +226,91 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             for (int i = 0; i < C::MAXK; ++i) {
                 const int kk = 2 * (tid + i * NT);
                 if (kk < 2 * npair) {
-                    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (l0 && P >= 2) acc = f4mul(xa[i], ha[i]);
-                    if ((l0 && P >= 3) || (!l0 && P >= 2)) acc = f4add(acc, ya[i]);
-                    *reinterpret_cast<float4*>(yacc + kk) = acc;
                     *reinterpret_cast<float4*>(h0s + kk) = h0a[i];
+                    if (use_x1) *reinterpret_cast<float4*>(yacc + kk) = ha[i];   // H_1 until X_{b-1} arrives
+                }
+            }
+        }
+    }
+
+    // earlier steps' kernels have completed and their writes are visible
+    cudaGridDependencySynchronize();
+
+    // ---- dynamic prologue: input ring, previous spectrum, partial sums and the
+    //      other levels' output rings (written by earlier steps) ---------------------
+    {
+        float4 wv[C::MAXQ];
+#pragma unroll
+        for (int i = 0; i < C::MAXQ; ++i) {
+            const int qd = tid + i * NT;
+            if (qd < nq_old) {
+                const long long ta = t_end - 2LL * N + 4LL * qd;
+                wv[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
+            }
+        }
+        float4 xa[C::PREFETCH ? C::MAXK : 1], ya[C::PREFETCH ? C::MAXK : 1];
+        float4 ev[C::PREFETCH ? C::MAXE : 1][kEmitLevels];
+        const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
+        if (C::PREFETCH) {
+#pragma unroll
+            for (int i = 0; i < C::MAXK; ++i) {
+                const int kk = 2 * (tid + i * NT);
+                if (kk < 2 * npair) {
+                    if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
+                    if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
                 }
             }
             if (l0) {
-                for (int L = kEmitLevels + 1; L < tk.M; ++L) {   // rare: more than 5 levels
-                    const DevLevel& l2 = bank.lv[tk.lv_index + L];
-#pragma unroll
-                    for (int i = 0; i < C::MAXE; ++i) {
-                        const int e4 = tid + i * NT;
-                        if (4 * e4 < N0)
-                            ev[i] = f4add(ev[i], __ldcg(reinterpret_cast<const float4*>(
-                                                     l2.yring + ((t_new + 4 * e4) & l2.rmask))));
-                    }
-                }
 #pragma unroll
                 for (int i = 0; i < C::MAXE; ++i) {
                     const int e4 = tid + i * NT;
-                    if (4 * e4 < N0) *reinterpret_cast<float4*>(emit + 4 * e4) = ev[i];
+#pragma unroll
+                    for (int L = 0; L < kEmitLevels; ++L)
+                        if (L < Le && 4 * e4 < N0)
+                            ev[i][L] = __ldcg(reinterpret_cast<const float4*>(
+                                tk.eyring[L] + ((t_new + 4 * e4) & tk.emask[L])));
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < C::MAXQ; ++i) {
+            const int qd = tid + i * NT;
+            if (qd < nq_old) {
+                s[2 * qd] = make_float2(wv[i].x, wv[i].y);
+                s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
+            } else if (l0 && qd < nq) {
+                // level 0 appends this step's input to the PC's ring (read back
+                // from the thread's own shared-memory writes)
+                const long long ta = t_end - 2LL * N + 4LL * qd;
+                const float2 a = s[2 * qd], bb = s[2 * qd + 1];
+                *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = make_float4(a.x, a.y, bb.x, bb.y);
+            }
+        }
+        if (C::PREFETCH) {
+#pragma unroll
+            for (int i = 0; i < C::MAXK; ++i) {
+                const int kk = 2 * (tid + i * NT);
+                if (kk < 2 * npair) {
+                    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (use_x1) acc = f4mul(xa[i], *reinterpret_cast<const float4*>(yacc + kk));
+                    if (use_yp) acc = f4add(acc, ya[i]);
+                    *reinterpret_cast<float4*>(yacc + kk) = acc;
+                }
+            }
+            if (l0) {
+#pragma unroll
+                for (int i = 0; i < C::MAXE; ++i) {
+                    const int e4 = tid + i * NT;
+                    if (4 * e4 >= N0) continue;
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int L = 0; L < kEmitLevels; ++L)
+                        if (L < Le) v = f4add(v, ev[i][L]);
+                    for (int L = kEmitLevels + 1; L < tk.M; ++L) {   // rare: more than 5 levels
+                        const DevLevel& l2 = bank.lv[tk.lv_index + L];
+                        v = f4add(v, __ldcg(reinterpret_cast<const float4*>(l2.yring + ((t_new + 4 * e4) & l2.rmask))));
+                    }
+                    *reinterpret_cast<float4*>(emit + 4 * e4) = v;
                 }
             }
         }
@@ -392,6 +436,9 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     __shared__ __align__(16) RunState rs;
     __shared__ int s_last;
     const int tid = threadIdx.x;
+    // the next step's CTAs may start their static prologue now; they wait in
+    // cudaGridDependencySynchronize() until this grid has completed
+    cudaTriggerProgrammaticLaunchCompletion();
     if (tid < 12) {
         reinterpret_cast<int4*>(&tk)[tid] = __ldg(reinterpret_cast<const int4*>(tasks + blockIdx.x) + tid);
     } else if (tid >= 32 && tid < 37) {
@@ -402,6 +449,7 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     __syncthreads();
     const long long c = rs.step_base + step_in_batch;
     if (tk.kind == 1) {
+        cudaGridDependencySynchronize();
         spread_body<C::NT>(tk, c, dyn_smem);
         return;
     }
@@ -482,13 +530,23 @@ cudaError_t prepare_kernels() {
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
                               const RunState* rs_dev, int step_in_batch, cudaStream_t st) {
     if (grid <= 0) return cudaSuccess;
-    const size_t smem = class_smem_bytes(cls, maxN);
+    // programmatic dependent launch: this step's CTAs may be scheduled while
+    // the previous kernel in the stream finishes (see cudaGridDependencySynchronize)
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kNT[cls]);
+    cfg.dynamicSmemBytes = class_smem_bytes(cls, maxN);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     switch (cls) {
-        case 0: step_kernel<Cls0><<<grid, Cls0::NT, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
-        case 1: step_kernel<Cls1><<<grid, Cls1::NT, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
-        default: step_kernel<Cls2><<<grid, Cls2::NT, smem, st>>>(bank, tasks, rs, rs_dev, step_in_batch); break;
+        case 0: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
+        case 1: return cudaLaunchKernelEx(&cfg, step_kernel<Cls1>, bank, tasks, rs, rs_dev, step_in_batch);
+        default: return cudaLaunchKernelEx(&cfg, step_kernel<Cls2>, bank, tasks, rs, rs_dev, step_in_batch);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,

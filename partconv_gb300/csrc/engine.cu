@@ -215,14 +215,18 @@ void free_device(pc_handle* h) {
 int phase_of(const pc_handle* h, long long step) { return (int)(step & (long long)(h->H - 1)); }
 
 // One base step by direct launches (classes with work in this phase).
-int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st) {
+// first: the preceding work in the stream is not one of this handle's step
+// kernels, so the launch must not overlap it.
+int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool first) {
     const int ph = phase_of(h, rs.step_base);
     for (int k = 0; k < kClasses; ++k) {
         const int cls = (h->l0_class + k) % kClasses;   // level-0 class first
         const int n = h->cnt[cls][ph];
         if (n <= 0) continue;
-        CK(launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs, nullptr, 0, st),
+        CK(launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs, nullptr, 0, st,
+                             !first),
            "step launch");
+        first = false;
         h->launches += 1;
     }
     return PC_OK;
@@ -253,7 +257,7 @@ int build_graph(pc_handle* h) {
             if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side[cls], fork, 0);
             if (e == cudaSuccess)
                 e = launch_step_class(cls, h->cnt[cls][ph], h->class_maxN[cls], h->bank,
-                                      h->d_tasks + h->off[cls][ph], dummy, h->d_rs, s, h->side[cls]);
+                                      h->d_tasks + h->off[cls][ph], dummy, h->d_rs, s, h->side[cls], false);
             cudaEvent_t join = mk();
             if (e == cudaSuccess) e = cudaEventRecord(join, h->side[cls]);
             joins.push_back(join);
@@ -262,7 +266,7 @@ int build_graph(pc_handle* h) {
         const int c0 = h->l0_class;
         if (e == cudaSuccess)
             e = launch_step_class(c0, h->cnt[c0][ph], h->class_maxN[c0], h->bank, h->d_tasks + h->off[c0][ph], dummy,
-                                  h->d_rs, s, h->stream);
+                                  h->d_rs, s, h->stream, s > 0);
         ++kernels;
         for (auto j : joins)
             if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, j, 0);
@@ -734,11 +738,13 @@ int run_steps(pc_handle* h, const IOView& view, long long nsteps, cudaStream_t s
     long long done = 0;
     RunState rs;
     rs.io = view;
+    bool first = true;   // the stream's preceding work is not a step kernel
     auto direct = [&](long long upto) -> int {
         for (; done < upto; ++done) {
             rs.step_base = h->frame_num + done;
-            int r = launch_step_direct(h, rs, st);
+            int r = launch_step_direct(h, rs, st, first);
             if (r) return r;
+            first = false;
         }
         return PC_OK;
     };
@@ -752,6 +758,7 @@ int run_steps(pc_handle* h, const IOView& view, long long nsteps, cudaStream_t s
         CK(cudaGraphLaunch(h->gexec, st), "graph launch");
         h->launches += 1 + h->graph_kernels;
         done += G;
+        first = true;
     }
     r = direct(nsteps);
     if (r) return r;
@@ -819,7 +826,11 @@ int process_device_impl(pc_handle* h, float* d_out, const float* d_in, long long
 // ===========================================================================
 // C ABI
 // ===========================================================================
-static std::string g_create_err;
+// errors of calls that have no handle (thread-local)
+static thread_local std::string g_global_err;
+const char* pcg_global_error() { return g_global_err.c_str(); }
+void pcg_set_global_error(const std::string& m) { g_global_err = m; }
+
 
 extern "C" {
 
@@ -838,7 +849,7 @@ int pc_check_layout(int M, const int* N, int* P, int ir_len, int relaxed, int* d
 pc_handle* pc_create(int verbosity) {
     pc_handle* h = new (std::nothrow) pc_handle();
     if (!h) {
-        g_create_err = "out of host memory";
+        pcg_set_global_error("out of host memory");
         return nullptr;
     }
     h->verbosity = verbosity;
@@ -989,7 +1000,7 @@ void pc_destroy(pc_handle* h) {
     delete h;
 }
 
-const char* pc_last_error(const pc_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+const char* pc_last_error(const pc_handle* h) { return h ? h->err.c_str() : pcg_global_error(); }
 
 int pc_get_info(const pc_handle* h, pc_info* info) {
     if (!h || !info) return PC_ERR_ARG;
@@ -1051,7 +1062,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
             cudaEventCreate(&r.b);
             cudaEventRecord(r.a, h->stream);
             cudaError_t e = launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs,
-                                              nullptr, 0, h->stream);
+                                              nullptr, 0, h->stream, false);
             cudaEventRecord(r.b, h->stream);
             recs.push_back(r);
             h->launches += 1;

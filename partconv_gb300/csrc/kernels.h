@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <string>
 
 #include "engine_types.h"
 
@@ -26,10 +27,16 @@ int spread_task_bins();
 size_t class_smem_bytes(int cls, int maxN);
 
 cudaError_t prepare_kernels();
+// pdl: let the launch overlap the previous kernel in the stream, which must
+// be a step kernel of the same handle (or nothing)
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
-                              const RunState* rs_dev, int step_in_batch, cudaStream_t st);
+                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl);
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,
                            cudaStream_t st);
 cudaError_t launch_set_state(RunState* dst, const RunState& v, cudaStream_t st);
 
 }  // namespace pcg
+
+// last error of calls that have no handle (thread-local)
+const char* pcg_global_error();
+void pcg_set_global_error(const std::string& m);

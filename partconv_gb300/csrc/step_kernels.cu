@@ -528,10 +528,12 @@ cudaError_t prepare_kernels() {
 }
 
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
-                              const RunState* rs_dev, int step_in_batch, cudaStream_t st) {
+                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl) {
     if (grid <= 0) return cudaSuccess;
     // programmatic dependent launch: this step's CTAs may be scheduled while
-    // the previous kernel in the stream finishes (see cudaGridDependencySynchronize)
+    // the previous step kernel in the stream finishes (their static prologue
+    // reads only data no step writes; see cudaGridDependencySynchronize).
+    // Callers pass pdl = false when the preceding work is anything else.
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
@@ -541,7 +543,7 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
     cfg.dynamicSmemBytes = class_smem_bytes(cls, maxN);
     cfg.stream = st;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = pdl ? 1 : 0;
     switch (cls) {
         case 0: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
         case 1: return cudaLaunchKernelEx(&cfg, step_kernel<Cls1>, bank, tasks, rs, rs_dev, step_in_batch);

@@ -186,6 +186,42 @@ typedef struct pc_kernel_stats {
  */
 int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int max_kinds, int* n_kinds);
 
+/* Size of the static device scratch array used by pc_convolve_noalloc. */
+#define PC_NOALLOC_SCRATCH_BYTES (32 << 20)
+
+/*
+ * Convolution for callers that cannot allocate device memory.  No
+ * counterpart in the reference: it exists for hosts that own every device
+ * allocation themselves -- a plug-in inside an application that accounts
+ * for all GPU memory, code under a memory pool or allocator that forbids
+ * cudaMalloc, or a real-time thread that must never block in the driver's
+ * allocator.
+ *
+ * Computes y[n] = sum_k h[k] x[n-k] for 0 <= n < n_frames from zero initial
+ * state, with the uniformly partitioned frequency-domain delay line of block
+ * size block_size (one level, ceil(h_len / block_size) parts); the result
+ * equals n_frames / block_size pc_run calls of a fresh handle set up with
+ * that layout.  d_x (n_frames samples), d_h (h_len taps) and d_y (n_frames
+ * samples) are device pointers owned by the caller; enqueued on `stream`
+ * (NULL = default stream), returns after enqueueing.
+ *
+ * All other working memory (filter spectra, spectrum ring, partial sums,
+ * input ring, task table, twiddles) is one file-scope device array of
+ * PC_NOALLOC_SCRATCH_BYTES (32 MiB) that every GPU loading this library
+ * holds until the process exits; the call allocates and frees nothing.  A
+ * layout needing more (about 2 * 8 * h_len bytes plus 0.3 MiB; e.g. IRs of
+ * up to ~1.9 M taps) fails with PC_ERR_LIMIT and a message from
+ * pc_last_error(NULL).  block_size: a power of two in [16, 1024].
+ *
+ * The first call on a device (that device current) resolves the array's
+ * device address with cudaGetSymbolAddress; make that first call before any
+ * stream capture.  Every call reuses the same array and clears the state it
+ * needs, so calls that overlap on the GPU (different streams, or different
+ * host threads on one device) race; serialise them.
+ */
+int pc_convolve_noalloc(const float* d_x, long long n_frames, const float* d_h, int h_len, float* d_y,
+                        int block_size, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

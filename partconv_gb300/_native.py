@@ -23,6 +23,7 @@ PC_INTERLEAVED = 0
 PC_PLANAR = 1
 PC_MAX_BLOCK = 16384
 PC_MAX_LEVELS = 16
+PC_NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _f32p = C.POINTER(C.c_float)
 _i32p = C.POINTER(C.c_int)
@@ -72,6 +73,8 @@ SIGNATURES = {
     "pc_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "pc_profile_kernels": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(PCKernelStats), C.c_int,
                                      C.POINTER(C.c_int)]),
+    "pc_convolve_noalloc": (C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                      C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -186,6 +186,56 @@ typedef struct pc_kernel_stats {
  */
 int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int max_kinds, int* n_kinds);
 
+/* ---------------------------------------------------------------------------
+ * PartConvFilter: one partitioned convolver driven level by level, the class
+ * the reference's Python module exposes (src/partconv.h:40-114, wrapped by
+ * src/partconv.i:3-12) and tune.py drives.  Same index state and DelayBuffer /
+ * DoubleBuffer schedule as the reference (src/partconv.cpp:354-648,
+ * :1401-1511); buffers and runLevel's FFT/MAC/IFFT run on the GPU.
+ * ------------------------------------------------------------------------- */
+typedef struct pcf_handle pcf_handle;
+
+/* PartConvFilter(verbosity, sampleRate) -- src/partconv.h:47. */
+pcf_handle* pcf_create(int verbosity, int sample_rate);
+
+/* PartConvFilter::setup(M, N, num_parts, impulse, fftwOptLevel, wisdom) --
+ * src/partconv.cpp:70-306.  ir == NULL benches with an all-ones IR of
+ * sum(N*P) taps (partconv.cpp:132-142).  Layout rules as pc_check_layout;
+ * relaxed_check = 0 is the reference's check.  P[M-1] is recomputed.
+ * Returns PC_ERR_LAYOUT where the reference returns 1. */
+int pcf_setup(pcf_handle* h, int M, const int* N, int* P, const float* ir, int ir_len, int relaxed_check);
+
+/* sync_levels() (relaxed = 0) / sync_levels_relaxed() (relaxed = 1) --
+ * src/partconv.cpp:568-603. */
+int pcf_sync_levels(pcf_handle* h, int relaxed);
+
+/* input(const float*) -- src/partconv.cpp:605-613: N[0] host samples. */
+int pcf_input(pcf_handle* h, const float* x);
+
+/* runLevel(L) -- src/partconv.cpp:354-490.  Where the reference exits on a
+ * DelayBuffer overlap (partconv.cpp:1449-1455) this returns PC_ERR_STATE. */
+int pcf_run_level(pcf_handle* h, int L);
+
+/* output(float*) (relaxed = 0) / output_relaxed(float*) (relaxed = 1) --
+ * src/partconv.cpp:616-648: N[0] host samples. */
+int pcf_output(pcf_handle* h, float* y, int relaxed);
+
+/* reset() -- src/partconv.cpp:492-506. */
+int pcf_reset(pcf_handle* h);
+
+/* bench(L, trials, pollute_every, max_time, benchData) --
+ * src/partconv.cpp:508-566: mean seconds of runLevel(L) (CUDA events);
+ * pollution writes a buffer larger than the GPU's L2.  Negative on error. */
+double pcf_bench(pcf_handle* h, int L, int trials, int pollute_every, double max_time, double* bench_data);
+
+/* cleanup() -- src/partconv.cpp:308-352; pcf_destroy frees the handle. */
+int pcf_cleanup(pcf_handle* h);
+void pcf_destroy(pcf_handle* h);
+const char* pcf_last_error(const pcf_handle* h);
+int pcf_get_parts(const pcf_handle* h, int* P);
+/* 1 if a runLevel found the DelayBuffer read and write blocks equal. */
+int pcf_overlap_error(const pcf_handle* h);
+
 /* Size of the static device scratch array used by pc_convolve_noalloc. */
 #define PC_NOALLOC_SCRATCH_BYTES (32 << 20)
 

@@ -75,6 +75,19 @@ SIGNATURES = {
                                      C.POINTER(C.c_int)]),
     "pc_convolve_noalloc": (C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                       C.c_void_p]),
+    "pcf_create": (C.c_void_p, [C.c_int, C.c_int]),
+    "pcf_setup": (C.c_int, [C.c_void_p, C.c_int, _i32p, _i32p, _f32p, C.c_int, C.c_int]),
+    "pcf_sync_levels": (C.c_int, [C.c_void_p, C.c_int]),
+    "pcf_input": (C.c_int, [C.c_void_p, _f32p]),
+    "pcf_run_level": (C.c_int, [C.c_void_p, C.c_int]),
+    "pcf_output": (C.c_int, [C.c_void_p, _f32p, C.c_int]),
+    "pcf_reset": (C.c_int, [C.c_void_p]),
+    "pcf_bench": (C.c_double, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]),
+    "pcf_cleanup": (C.c_int, [C.c_void_p]),
+    "pcf_destroy": (None, [C.c_void_p]),
+    "pcf_last_error": (C.c_char_p, [C.c_void_p]),
+    "pcf_get_parts": (C.c_int, [C.c_void_p, _i32p]),
+    "pcf_overlap_error": (C.c_int, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

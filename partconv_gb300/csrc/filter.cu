@@ -438,7 +438,8 @@ int pcf_reset(pcf_handle* h) {
         FCK(cudaMemsetAsync(d.d_mem, 0, sizeof(float) * (size_t)d.bufferSize * d.frameSize, h->stream), "reset");
         d.init_indices();
     }
-    FCK(cudaMemsetAsync(h->out0, 0, sizeof(float) * h->N[0], h->stream), "reset");
+    // like the reference, reset leaves level 0's last block (outbuffer[0])
+    // in place: the first output_relaxed() after a reset returns it
     FCK(cudaStreamSynchronize(h->stream), "reset sync");
     h->overlap_error = false;
     return PC_OK;

@@ -225,10 +225,9 @@ def test_delay_and_double_buffer_semantics(gpu):
     # readFrameDelay = 2: after writing frame i (value i+1) the block read
     # holds frames i-2 and i-1 (zeros before the first writes)
     assert got == [[0, 0], [1, 2], [3, 4], [5, 6], [7, 8], [9, 10]]
+    d2 = partconv.DelayBuffer(4, 1, 2)   # 3 one-frame blocks: read 2, write 0
+    d2.prepNextRead()                    # read block 0 == write block 0
     with pytest.raises(partconv.PartConvError):
-        d2 = partconv.DelayBuffer(4, 1, 2)
-        d2.prepNextRead()
-        d2.prepNextRead()
         d2.read()
     dbuf = partconv.DoubleBuffer(8)
     dbuf.getWriteBuffer().fill_(2.0)

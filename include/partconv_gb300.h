@@ -236,6 +236,34 @@ int pcf_get_parts(const pcf_handle* h, int* P);
 /* 1 if a runLevel found the DelayBuffer read and write blocks equal. */
 int pcf_overlap_error(const pcf_handle* h);
 
+/* ---------------------------------------------------------------------------
+ * MIMO convolution: n_in inputs, n_out outputs, y_o = sum_i x_i * h_{i,o},
+ * all paths with one layout.  No reference counterpart as one object: the
+ * reference runs one PartConvFilter per path and sums outputs in time
+ * (src/partconvMulti.cpp:911-921); here each input's spectrum is computed
+ * once and every output's FDL sums over inputs per frequency bin.
+ * ------------------------------------------------------------------------- */
+typedef struct pcm_handle pcm_handle;
+
+pcm_handle* pcm_create(int verbosity);
+
+/* irs: n_in * n_out * ir_len floats, path (i, o) at (i * n_out + o) * ir_len.
+ * N/P as in pc_setup_layout (relaxed check; P[M-1] recomputed in place). */
+int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M, const int* N, int* P,
+              const float* irs, int ir_len);
+
+/* frames (a multiple of buffer_size) of device input -> device output,
+ * PC_INTERLEAVED or PC_PLANAR, enqueued on stream (NULL = default). */
+int pcm_process_device(pcm_handle* h, float* d_out, const float* d_in, long long frames, int layout,
+                       void* stream);
+int pcm_reset(pcm_handle* h);
+/* Per-kernel CUDA-event timing (names "mimo_xfft", "mimo_mac", "mimo_yifft"). */
+int pcm_profile_kernels(pcm_handle* h, long long nsteps, pc_kernel_stats* out, int max_kinds, int* n_kinds);
+long long pcm_device_bytes(const pcm_handle* h);
+long long pcm_kernel_launches(const pcm_handle* h);
+const char* pcm_last_error(const pcm_handle* h);
+void pcm_destroy(pcm_handle* h);
+
 /* Size of the static device scratch array used by pc_convolve_noalloc. */
 #define PC_NOALLOC_SCRATCH_BYTES (32 << 20)
 

@@ -88,6 +88,16 @@ SIGNATURES = {
     "pcf_last_error": (C.c_char_p, [C.c_void_p]),
     "pcf_get_parts": (C.c_int, [C.c_void_p, _i32p]),
     "pcf_overlap_error": (C.c_int, [C.c_void_p]),
+    "pcm_create": (C.c_void_p, [C.c_int]),
+    "pcm_setup": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i32p, _i32p, _f32p, C.c_int]),
+    "pcm_process_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "pcm_reset": (C.c_int, [C.c_void_p]),
+    "pcm_profile_kernels": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(PCKernelStats), C.c_int,
+                                      C.POINTER(C.c_int)]),
+    "pcm_device_bytes": (C.c_longlong, [C.c_void_p]),
+    "pcm_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "pcm_last_error": (C.c_char_p, [C.c_void_p]),
+    "pcm_destroy": (None, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -48,6 +48,7 @@ constexpr int kMacNT = 256;        // MAC CTA: 4 groups x 64 lanes, two bins per
 constexpr int kMacLanes = 64;
 constexpr int kMacBins = 2 * kMacLanes;
 constexpr int kMaxMimoLevels = 8;
+constexpr int kMaxMacTerms = 2048;  // (input, part) terms one MAC task sums
 
 struct MLevel {
     int N, logN, P, T, s_blocks, cs, rmask, npart;
@@ -175,9 +176,21 @@ __global__ void __launch_bounds__(kMacNT) mimo_mac_kernel(const MBank* __restric
         ni = t.i1 - t.i0;
     }
     const int J = ni * np;
-    const size_t rowX = (size_t)cs, rowH = (size_t)cs;
-    const float2* Hbase = l.H + (size_t)o * nI * P * rowH + k;
-    const float2* Xbase = l.X + k;
+    // row offsets (in float4 units) of every (input, part) term, computed
+    // once per CTA so the streaming loop carries no index arithmetic
+    __shared__ int xoff[kMaxMacTerms], hoff[kMaxMacTerms];
+    const int slot_bt = (int)imod(bt, P);
+    for (int j = threadIdx.x; j < J; j += kMacNT) {
+        const int i = i0 + j / np;
+        const int p = p_lo + j % np;
+        int sl = slot_bt - p;
+        if (sl < 0) sl += P;
+        xoff[j] = ((i * P + sl) * cs) >> 1;
+        hoff[j] = ((i * P + p) * cs) >> 1;
+    }
+    __syncthreads();
+    const float4* H4 = reinterpret_cast<const float4*>(l.H + (size_t)o * nI * P * cs + k);
+    const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
         constexpr int U = 8;
@@ -187,11 +200,8 @@ __global__ void __launch_bounds__(kMacNT) mimo_mac_kernel(const MBank* __restric
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u * G;
                 if (j < J) {
-                    const int i = i0 + j / np;
-                    const int p = p_lo + j % np;
-                    const int sl = (int)imod(bt - p, P);
-                    xv[u] = __ldcg(reinterpret_cast<const float4*>(Xbase + ((size_t)i * P + sl) * rowX));
-                    hv[u] = __ldcs(reinterpret_cast<const float4*>(Hbase + ((size_t)i * P + p) * rowH));
+                    xv[u] = __ldcg(X4 + xoff[j]);
+                    hv[u] = __ldcs(H4 + hoff[j]);
                 }
             }
 #pragma unroll
@@ -500,8 +510,16 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
         long R = Nv[L];
         while (R < s + buffer_size) R <<= 1;
         l.rmask = (int)R - 1;
-        // input ranges per spread task: about 8 inputs each
+        // input ranges per spread task (about 8 inputs each, more ranges when
+        // a range times the older parts exceeds what one MAC task sums)
+        const int p_lo = l.T == 1 ? 2 : 1;
         l.npart = std::max(1, std::min(n_in, 8));
+        while (l.npart < n_in && (long)((n_in + l.npart - 1) / l.npart) * std::max(l.P - p_lo, 0) > kMaxMacTerms)
+            l.npart *= 2;
+        l.npart = std::min(l.npart, n_in);
+        if ((long)((n_in + l.npart - 1) / l.npart) * std::max(l.P - p_lo, 0) > kMaxMacTerms ||
+            (long)n_in * 2 > kMaxMacTerms || (long)n_in * l.P * l.cs >= (1L << 31))
+            return mfail(h, PC_ERR_LIMIT, "MIMO layout too large for one MAC task (inputs x parts)");
         MCK(malloc_zero(h, &l.H, (size_t)n_out * n_in * l.P * l.cs, false), "alloc H");
         MCK(malloc_zero(h, &l.X, (size_t)n_in * l.P * l.cs, true), "alloc");
         MCK(malloc_zero(h, &l.Yp, (size_t)n_out * l.npart * 2 * l.cs, true), "alloc");

@@ -264,6 +264,34 @@ long long pcm_kernel_launches(const pcm_handle* h);
 const char* pcm_last_error(const pcm_handle* h);
 void pcm_destroy(pcm_handle* h);
 
+/* ---------------------------------------------------------------------------
+ * Differentiable partitioned convolution (no reference counterpart: the
+ * reference has no gradients).  y_s = (x_s * h)[0:T] for a batch of signals,
+ * all blocks of a level computed in parallel, and hand-written adjoints:
+ * dL/dx with conjugated filter spectra (anti-causal), dL/dh as a partitioned
+ * cross-correlation of the input with dL/dy in the same layout.
+ * ------------------------------------------------------------------------- */
+typedef struct pcd_plan pcd_plan;
+
+/* Layout as pc_check_layout (relaxed; P[M-1] recomputed); batch signals of
+ * `length` samples; h of ir_len taps.  NULL on error (message in msg). */
+pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long long length, char* msg,
+                     int msglen);
+/* Device workspace the caller provides to forward/backward (no allocation
+ * inside); forward leaves filter and input spectra in it for backward. */
+long long pcd_workspace_bytes(const pcd_plan* p);
+/* y[batch][length] from x[batch][length] and h[ir_len] (device pointers). */
+int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, void* d_ws, void* stream);
+/* dL/dx (d_gx, may be NULL) and dL/dh (d_gh, may be NULL) from dL/dy.
+ * recompute = 1 rebuilds the spectra from x and h instead of reading the
+ * ones the forward pass left (needed when the workspace was reused, and for
+ * a second backward: the adjoint pass overwrites the input spectra). */
+int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d_gy, float* d_gx, float* d_gh,
+                 void* d_ws, int recompute, void* stream);
+void pcd_destroy(pcd_plan* p);
+const char* pcd_last_error(const pcd_plan* p);
+long long pcd_kernel_launches(const pcd_plan* p);
+
 /* Size of the static device scratch array used by pc_convolve_noalloc. */
 #define PC_NOALLOC_SCRATCH_BYTES (32 << 20)
 

@@ -98,6 +98,14 @@ SIGNATURES = {
     "pcm_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "pcm_last_error": (C.c_char_p, [C.c_void_p]),
     "pcm_destroy": (None, [C.c_void_p]),
+    "pcd_create": (C.c_void_p, [C.c_int, _i32p, _i32p, C.c_int, C.c_int, C.c_longlong, C.c_char_p, C.c_int]),
+    "pcd_workspace_bytes": (C.c_longlong, [C.c_void_p]),
+    "pcd_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pcd_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_int, C.c_void_p]),
+    "pcd_destroy": (None, [C.c_void_p]),
+    "pcd_last_error": (C.c_char_p, [C.c_void_p]),
+    "pcd_kernel_launches": (C.c_longlong, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,475 @@
+// adjoint.cu -- differentiable partitioned convolution: block-parallel FDL
+// forward pass and hand-written adjoint kernels.
+//
+// For a batch of signals x_s (length T) and one IR h, y_s = (x_s * h)[0:T]
+// with the IR cut into the levels of a partition layout (level L: N_L-sample
+// blocks, P_L parts, taps [s_L, s_L + N_L P_L)).  The whole signal is known,
+// so every block of a level is computed in parallel (offline form of the
+// streaming FDL of PartConvFilter::runLevel, src/partconv.cpp:354-490):
+//   X_b  = rfft(x_L window [(b-1)N, (b+1)N)),  x_L[m] = x[m - s_L]
+//   Y_b  = sum_p X_{b-p} H_p,  H_p = rfft([0_N, h_p]) / 2N
+//   y_L block b = irfft(Y_b)[0:N]
+// Backward with g = dL/dy:
+//   dL/dx (adjoint, anti-causal, conjugated spectra):
+//     G'_c = rfft(g[cN + s_L, cN + s_L + 2N)),
+//     gx_L block b = irfft(sum_p (-1)^k conj(H_p) G'_{b+p})[0:N]
+//   dL/dh (partitioned cross-correlation of the input with the gradient):
+//     GP_b = rfft([g block b, 0_N]),  D_p = sum_s sum_b conj(GP_b) X_{b-p},
+//     dh[s_L + pN + q] = irfft(D_p)[N - q] / 2N,  0 <= q < N.
+// Levels are summed in ascending order (PartConvFilter::output,
+// src/partconv.cpp:616-631).  The caller provides the workspace (no
+// allocation here); the input spectra X can be kept from the forward pass or
+// recomputed in the backward pass.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/partconv_gb300.h"
+#include "engine_types.h"
+#include "fft_smem.cuh"
+#include "kernels.h"
+
+using namespace pcg;
+
+namespace {
+
+constexpr int kWlog = 15;
+constexpr int kMaxDLevels = 8;
+constexpr int kDhChunks = 16;   // partial sums of the dL/dh reduction (fixed order)
+
+// window FFT job: dst = rfft(w) * scale, w[n] = src[start + n] for n < 2N,
+// zero outside [0, len); half == 1 zeroes the second half ([g block, 0_N]),
+// half == 2 the first half ([0_N, h part])
+struct FJob {
+    const float* src;
+    long long len, start;
+    float2* dst;
+    float scale;
+    int half;
+};
+// inverse FFT job: out = irfft(src); mode 0: dst[i] = out[i], 1: dst[i] += out[i]
+// (i < min(N, limit)); mode 2: dst[q] = out[N - q] * scale (q < min(N, limit))
+struct IJob {
+    const float2* src;
+    float* dst;
+    long long limit;
+    float scale;
+    int mode;
+};
+
+template <int NT, int MAXB>
+__global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs, int N, int logN, const float2* W,
+                                                  int wlog) {
+    extern __shared__ float4 dyn_smem[];
+    float2* s = reinterpret_cast<float2*>(dyn_smem);
+    float2* twt = s + N;
+    const FJob jb = jobs[blockIdx.x];
+    const int lo = jb.half == 2 ? N : 0, hi = jb.half == 1 ? N : 2 * N;   // live window samples [lo, hi)
+    for (int n = threadIdx.x; n < N; n += NT) {
+        const long long i = jb.start + 2LL * n;
+        float a = 0.f, b = 0.f;
+        if (2 * n >= lo && 2 * n < hi && i >= 0 && i < jb.len) a = jb.src[i];
+        if (2 * n + 1 >= lo && 2 * n + 1 < hi && i + 1 >= 0 && i + 1 < jb.len) b = jb.src[i + 1];
+        s[n] = make_float2(a, b);
+    }
+    load_twiddles<NT>(twt, logN, W, wlog);
+    __syncthreads();
+    const Twiddles tw{twt, logN};
+    fft_smem<NT, MAXB>(s, N, logN, tw, false);
+    for (int k = threadIdx.x; k <= N / 2; k += NT) {
+        const int nk = (k == 0) ? 0 : N - k;
+        float2 xk, xnk;
+        rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
+        jb.dst[k] = make_float2(xk.x * jb.scale, xk.y * jb.scale);
+        if (N - k != k) jb.dst[N - k] = make_float2(xnk.x * jb.scale, xnk.y * jb.scale);
+    }
+}
+
+template <int NT, int MAXB>
+__global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs, int N, int logN, const float2* W,
+                                                   int wlog) {
+    extern __shared__ float4 dyn_smem[];
+    float2* s = reinterpret_cast<float2*>(dyn_smem);
+    float2* twt = s + N;
+    const IJob jb = jobs[blockIdx.x];
+    load_twiddles<NT>(twt, logN, W, wlog);
+    __syncthreads();
+    const Twiddles tw{twt, logN};
+    for (int k = threadIdx.x; k <= N / 2; k += NT) {
+        float2 zk, znk;
+        irfft_merge(jb.src[k], jb.src[N - k], k, logN, tw, zk, znk);
+        s[k] = zk;
+        if (k != 0 && k != N / 2) s[N - k] = znk;
+    }
+    __syncthreads();
+    fft_smem<NT, MAXB>(s, N, logN, tw, true);
+    const float* sf = reinterpret_cast<const float*>(s);
+    const int n = jb.limit < N ? (int)jb.limit : N;
+    for (int i = threadIdx.x; i < n; i += NT) {
+        if (jb.mode == 0) jb.dst[i] = sf[i];
+        else if (jb.mode == 1) jb.dst[i] += sf[i];
+        else jb.dst[i] = sf[N - i] * jb.scale;
+    }
+}
+
+// Y[s][b] = sum_p X[s][b-p] H[p]                       (forward, mode 0)
+// Y[s][b] = sum_p (-1)^k conj(H[p]) X[s][b+p]          (adjoint, mode 1)
+// X has nxb blocks per signal; Y has nyb.
+__global__ void dmac_kernel(const float2* __restrict__ X, const float2* __restrict__ H, float2* __restrict__ Y, int nsig,
+                            int nxb, int nyb, int P, int cs, int mode) {
+    const long long total = (long long)nsig * nyb * cs;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % cs);
+        const long long sb = t / cs;
+        const int b = (int)(sb % nyb);
+        const int sg = (int)(sb / nyb);
+        float2 acc = make_float2(0.f, 0.f);
+        for (int p = 0; p < P; ++p) {
+            const int xb = mode == 0 ? b - p : b + p;
+            if (xb < 0 || xb >= nxb) continue;
+            const float2 x = X[((long long)sg * nxb + xb) * cs + k];
+            float2 h = H[(long long)p * cs + k];
+            if (mode == 1) h = (k & 1) ? make_float2(-h.x, h.y) : make_float2(h.x, -h.y);   // (-1)^k conj(h)
+            acc = cadd(acc, cmul(x, h));
+        }
+        Y[t] = acc;
+    }
+}
+
+// Dpart[chunk][p][k] = sum over (s, b) of chunk of conj(GP[s][b][k]) X[s][b-p][k]
+__global__ void ddh_partial_kernel(const float2* __restrict__ X, const float2* __restrict__ GP,
+                                   float2* __restrict__ Dpart, int nsig, int nb, int P, int cs, int nchunk) {
+    const long long total = (long long)nchunk * P * cs;
+    const long long nsb = (long long)nsig * nb;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % cs);
+        const int p = (int)((t / cs) % P);
+        const int ch = (int)(t / ((long long)cs * P));
+        const long long j0 = ch * nsb / nchunk, j1 = (ch + 1) * nsb / nchunk;
+        float2 acc = make_float2(0.f, 0.f);
+        for (long long j = j0; j < j1; ++j) {
+            const int sg = (int)(j / nb), b = (int)(j % nb);
+            if (b - p < 0) continue;
+            const float2 g = GP[((long long)sg * nb + b) * cs + k];
+            const float2 x = X[((long long)sg * nb + (b - p)) * cs + k];
+            acc = cadd(acc, cmul(cconj(g), x));
+        }
+        Dpart[t] = acc;
+    }
+}
+
+__global__ void ddh_reduce_kernel(const float2* __restrict__ Dpart, float2* __restrict__ D, int P, int cs, int nchunk) {
+    const int total = P * cs;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int c = 0; c < nchunk; ++c) acc = cadd(acc, Dpart[(long long)c * total + t]);
+        D[t] = acc;
+    }
+}
+
+int cls_of(int N) { return N <= 1024 ? 0 : (N <= 4096 ? 1 : 2); }
+
+cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const float2* W, cudaStream_t st) {
+    if (njobs <= 0) return cudaSuccess;
+    const size_t smem = (size_t)12 * N;
+    switch (cls_of(N)) {
+        case 0: dfft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, N, logN, W, kWlog); break;
+        case 1: dfft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
+        default: dfft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ifft(int N, int logN, const IJob* jobs, int njobs, const float2* W, cudaStream_t st) {
+    if (njobs <= 0) return cudaSuccess;
+    const size_t smem = (size_t)12 * N;
+    switch (cls_of(N)) {
+        case 0: difft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, N, logN, W, kWlog); break;
+        case 1: difft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
+        default: difft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+struct pcd_plan {
+    int M = 0, B = 0, ir_len = 0;
+    long long T = 0;
+    std::vector<int> N, P, logN, cs, nb, nbg;
+    std::vector<long long> s;
+    // workspace offsets (bytes)
+    size_t o_W = 0, o_jobs = 0, o_ijobs = 0, total = 0;
+    std::vector<size_t> o_H, o_X, o_Y, o_Dp, o_D;
+    size_t njobs_max = 0;
+    std::string err;
+    long long launches = 0;
+};
+
+namespace {
+
+size_t take(size_t& off, size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+}
+
+int dfail(pcd_plan* p, int code, const std::string& m) {
+    if (p) p->err = m;
+    return code;
+}
+
+#define DCK(call, where)                                                                                   \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess) return dfail(p, PC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct WS {
+    char* base;
+    template <class T>
+    T* at(size_t off) const {
+        return reinterpret_cast<T*>(base + off);
+    }
+};
+
+// upload a job table into the workspace and launch
+int run_fft_jobs(pcd_plan* p, const WS& w, int L, const std::vector<FJob>& jobs, cudaStream_t st) {
+    if (jobs.empty()) return PC_OK;
+    FJob* d = w.at<FJob>(p->o_jobs);
+    DCK(cudaMemcpyAsync(d, jobs.data(), sizeof(FJob) * jobs.size(), cudaMemcpyHostToDevice, st), "job upload");
+    DCK(launch_fft(p->N[L], p->logN[L], d, (int)jobs.size(), w.at<float2>(p->o_W), st), "window FFT");
+    p->launches++;
+    // the job table is reused by the next call: order the host writes after this launch
+    DCK(cudaStreamSynchronize(st), "job sync");
+    return PC_OK;
+}
+
+int run_ifft_jobs(pcd_plan* p, const WS& w, int L, const std::vector<IJob>& jobs, cudaStream_t st) {
+    if (jobs.empty()) return PC_OK;
+    IJob* d = w.at<IJob>(p->o_ijobs);
+    DCK(cudaMemcpyAsync(d, jobs.data(), sizeof(IJob) * jobs.size(), cudaMemcpyHostToDevice, st), "job upload");
+    DCK(launch_ifft(p->N[L], p->logN[L], d, (int)jobs.size(), w.at<float2>(p->o_W), st), "inverse FFT");
+    p->launches++;
+    DCK(cudaStreamSynchronize(st), "job sync");
+    return PC_OK;
+}
+
+int filter_spectra(pcd_plan* p, const WS& w, const float* d_h, cudaStream_t st) {
+    for (int L = 0; L < p->M; ++L) {
+        std::vector<FJob> jobs;
+        for (int q = 0; q < p->P[L]; ++q)   // row [0_N, h_q]: the window starts N before the part
+            jobs.push_back(FJob{d_h, p->ir_len, p->s[L] + (long long)q * p->N[L] - p->N[L],
+                                w.at<float2>(p->o_H[L]) + (size_t)q * p->cs[L], 1.0f / (2.0f * p->N[L]), 2});
+        int r = run_fft_jobs(p, w, L, jobs, st);
+        if (r) return r;
+    }
+    return PC_OK;
+}
+
+int input_spectra(pcd_plan* p, const WS& w, const float* d_x, cudaStream_t st) {
+    for (int L = 0; L < p->M; ++L) {
+        std::vector<FJob> jobs;
+        for (int sg = 0; sg < p->B; ++sg)
+            for (int b = 0; b < p->nb[L]; ++b)
+                jobs.push_back(FJob{d_x + (size_t)sg * p->T, p->T, (long long)(b - 1) * p->N[L] - p->s[L],
+                                    w.at<float2>(p->o_X[L]) + ((size_t)sg * p->nb[L] + b) * p->cs[L], 1.0f, 0});
+        int r = run_fft_jobs(p, w, L, jobs, st);
+        if (r) return r;
+    }
+    return PC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long long length, char* msg, int msglen) {
+    auto put = [&](const char* m) {
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", m);
+    };
+    if (M < 1 || M > kMaxDLevels || !N || !P || ir_len < 1 || batch < 1 || length < 1) {
+        put("bad plan arguments");
+        return nullptr;
+    }
+    std::vector<int> Nv(N, N + M), Pv(P, P + M);
+    char m2[256];
+    if (pc_check_layout(M, Nv.data(), Pv.data(), ir_len, 1, nullptr, m2, sizeof m2)) {
+        put(m2);
+        return nullptr;
+    }
+    if (Nv[0] < 16) {
+        put("block size of level 0 must be >= 16");
+        return nullptr;
+    }
+    for (int i = 0; i < M; ++i) P[i] = Pv[i];
+    pcd_plan* p = new (std::nothrow) pcd_plan();
+    if (!p) return nullptr;
+    p->M = M;
+    p->B = batch;
+    p->ir_len = ir_len;
+    p->T = length;
+    p->N = Nv;
+    p->P = Pv;
+    long long s = 0;
+    size_t off = 0;
+    p->o_W = take(off, sizeof(float2) << kWlog);
+    for (int L = 0; L < M; ++L) {
+        p->s.push_back(s);
+        p->logN.push_back((int)std::lround(std::log2((double)Nv[L])));
+        p->cs.push_back(Nv[L] + 2);
+        const int nb = (int)((length + Nv[L] - 1) / Nv[L]);
+        p->nb.push_back(nb);
+        p->nbg.push_back(nb + Pv[L] - 1);   // adjoint windows reach P-1 blocks past the end
+        s += (long long)Nv[L] * Pv[L];
+    }
+    size_t maxjobs = 0;
+    for (int L = 0; L < M; ++L) {
+        const size_t cs = p->cs[L];
+        p->o_H.push_back(take(off, sizeof(float2) * Pv[L] * cs));
+        p->o_X.push_back(take(off, sizeof(float2) * (size_t)batch * p->nb[L] * cs));
+        p->o_Y.push_back(take(off, sizeof(float2) * (size_t)batch * p->nbg[L] * cs));
+        p->o_Dp.push_back(take(off, sizeof(float2) * (size_t)kDhChunks * Pv[L] * cs));
+        p->o_D.push_back(take(off, sizeof(float2) * (size_t)Pv[L] * cs));
+        maxjobs = std::max(maxjobs, (size_t)batch * p->nbg[L]);
+        maxjobs = std::max(maxjobs, (size_t)Pv[L]);
+    }
+    p->njobs_max = maxjobs;
+    p->o_jobs = take(off, sizeof(FJob) * maxjobs);
+    p->o_ijobs = take(off, sizeof(IJob) * maxjobs);
+    p->total = off;
+    put("");
+    return p;
+}
+
+long long pcd_workspace_bytes(const pcd_plan* p) { return p ? (long long)p->total : -1; }
+
+int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, void* d_ws, void* stream) {
+    if (!p || !d_x || !d_h || !d_y || !d_ws) return dfail(p, PC_ERR_ARG, "null pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    WS w{static_cast<char*>(d_ws)};
+    {
+        static thread_local std::vector<float2> Wh;
+        if (Wh.empty()) {
+            Wh.resize((size_t)1 << kWlog);
+            for (size_t m = 0; m < Wh.size(); ++m) {
+                const double a = -2.0 * M_PI * (double)m / (double)Wh.size();
+                Wh[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+            }
+        }
+        DCK(cudaMemcpyAsync(w.at<float2>(p->o_W), Wh.data(), sizeof(float2) * Wh.size(), cudaMemcpyHostToDevice, st),
+            "twiddles");
+    }
+    for (int L = 0; L < p->M; ++L) {
+        DCK(cudaFuncSetAttribute(dfft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
+        DCK(cudaFuncSetAttribute(difft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
+        break;
+    }
+    int r = filter_spectra(p, w, d_h, st);
+    if (r) return r;
+    r = input_spectra(p, w, d_x, st);
+    if (r) return r;
+    for (int L = 0; L < p->M; ++L) {
+        const int cs = p->cs[L], nb = p->nb[L];
+        float2* Y = w.at<float2>(p->o_Y[L]);
+        const long long total = (long long)p->B * nb * cs;
+        dmac_kernel<<<(int)std::min<long long>((total + 255) / 256, 152 * 16), 256, 0, st>>>(
+            w.at<float2>(p->o_X[L]), w.at<float2>(p->o_H[L]), Y, p->B, nb, nb, p->P[L], cs, 0);
+        DCK(cudaGetLastError(), "forward MAC");
+        p->launches++;
+        std::vector<IJob> jobs;
+        for (int sg = 0; sg < p->B; ++sg)
+            for (int b = 0; b < nb; ++b) {
+                const long long t0 = (long long)b * p->N[L];
+                jobs.push_back(IJob{Y + ((size_t)sg * nb + b) * cs, d_y + (size_t)sg * p->T + t0, p->T - t0, 1.0f,
+                                    L == 0 ? 0 : 1});
+            }
+        r = run_ifft_jobs(p, w, L, jobs, st);
+        if (r) return r;
+    }
+    return PC_OK;
+}
+
+int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d_gy, float* d_gx, float* d_gh,
+                 void* d_ws, int recompute, void* stream) {
+    if (!p || !d_gy || !d_ws) return dfail(p, PC_ERR_ARG, "null pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    WS w{static_cast<char*>(d_ws)};
+    int r;
+    if (recompute) {   // rebuild what the forward pass left in the workspace
+        if (!d_x || !d_h) return dfail(p, PC_ERR_ARG, "recompute needs x and h");
+        r = filter_spectra(p, w, d_h, st);
+        if (r) return r;
+        r = input_spectra(p, w, d_x, st);
+        if (r) return r;
+    }
+    for (int L = 0; L < p->M; ++L) {
+        const int N = p->N[L], cs = p->cs[L], nb = p->nb[L], nbg = p->nbg[L], P = p->P[L];
+        float2* Y = w.at<float2>(p->o_Y[L]);
+        // dL/dh first: it needs the input spectra X, which the adjoint pass
+        // below overwrites with its own result
+        if (d_gh) {
+            std::vector<FJob> fj;   // GP_b = rfft([g block b, 0_N])
+            for (int sg = 0; sg < p->B; ++sg)
+                for (int b = 0; b < nb; ++b)
+                    fj.push_back(FJob{d_gy + (size_t)sg * p->T, p->T, (long long)b * N, Y + ((size_t)sg * nb + b) * cs,
+                                      1.0f, 1});
+            r = run_fft_jobs(p, w, L, fj, st);
+            if (r) return r;
+            float2* Dp = w.at<float2>(p->o_Dp[L]);
+            float2* D = w.at<float2>(p->o_D[L]);
+            const long long tot = (long long)kDhChunks * P * cs;
+            ddh_partial_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152 * 16), 256, 0, st>>>(
+                w.at<float2>(p->o_X[L]), Y, Dp, p->B, nb, P, cs, kDhChunks);
+            ddh_reduce_kernel<<<(P * cs + 255) / 256, 256, 0, st>>>(Dp, D, P, cs, kDhChunks);
+            DCK(cudaGetLastError(), "dL/dh reduction");
+            p->launches += 2;
+            std::vector<IJob> ij;   // dh[s_L + qN + t] = irfft(D_q)[N - t] / 2N
+            for (int q = 0; q < P; ++q) {
+                const long long t0 = p->s[L] + (long long)q * N;
+                if (t0 >= p->ir_len) break;
+                ij.push_back(IJob{D + (size_t)q * cs, d_gh + t0, p->ir_len - t0, 1.0f / (2.0f * N), 2});
+            }
+            r = run_ifft_jobs(p, w, L, ij, st);
+            if (r) return r;
+        }
+        if (d_gx) {
+            std::vector<FJob> fj;   // G'_c = rfft(g[cN + s_L, cN + s_L + 2N)), c < nb + P - 1
+            for (int sg = 0; sg < p->B; ++sg)
+                for (int c = 0; c < nbg; ++c)
+                    fj.push_back(FJob{d_gy + (size_t)sg * p->T, p->T, (long long)c * N + p->s[L],
+                                      Y + ((size_t)sg * nbg + c) * cs, 1.0f, 0});
+            r = run_fft_jobs(p, w, L, fj, st);
+            if (r) return r;
+            float2* Z = w.at<float2>(p->o_X[L]);   // adjoint sums replace the input spectra
+            const long long total = (long long)p->B * nb * cs;
+            dmac_kernel<<<(int)std::min<long long>((total + 255) / 256, 152 * 16), 256, 0, st>>>(
+                Y, w.at<float2>(p->o_H[L]), Z, p->B, nbg, nb, P, cs, 1);
+            DCK(cudaGetLastError(), "adjoint MAC");
+            p->launches++;
+            std::vector<IJob> ij;
+            for (int sg = 0; sg < p->B; ++sg)
+                for (int b = 0; b < nb; ++b) {
+                    const long long t0 = (long long)b * N;
+                    ij.push_back(IJob{Z + ((size_t)sg * nb + b) * cs, d_gx + (size_t)sg * p->T + t0, p->T - t0, 1.0f,
+                                      L == 0 ? 0 : 1});
+                }
+            r = run_ifft_jobs(p, w, L, ij, st);
+            if (r) return r;
+        }
+    }
+    return PC_OK;
+}
+
+void pcd_destroy(pcd_plan* p) { delete p; }
+const char* pcd_last_error(const pcd_plan* p) { return p ? p->err.c_str() : ""; }
+long long pcd_kernel_launches(const pcd_plan* p) { return p ? p->launches : 0; }
+
+}  // extern "C"

@@ -292,6 +292,33 @@ void pcd_destroy(pcd_plan* p);
 const char* pcd_last_error(const pcd_plan* p);
 long long pcd_kernel_launches(const pcd_plan* p);
 
+/* ---------------------------------------------------------------------------
+ * Serving pool (no reference counterpart: the reference's PartConvMulti is
+ * fixed at setup).  Partitioned convolvers of one base block size join and
+ * leave between steps; their spectra and FDL state live in one device arena
+ * of hbm_budget_bytes, and admission beyond it is refused (PC_ERR_NOMEM) so
+ * the caller can queue the request.  Each pcs_step advances every active PC
+ * by one base block in one batched launch per block-size class.
+ * ------------------------------------------------------------------------- */
+typedef struct pcs_handle pcs_handle;
+
+/* buffer_size: a power of two in [16, 1024]; max_pcs: channel capacity. */
+pcs_handle* pcs_create(int buffer_size, long long hbm_budget_bytes, int max_pcs);
+/* Admit one PC (IR, layout as pc_check_layout, at most 5 levels); its id is
+ * also its I/O channel.  Its schedule starts at the pool's next step. */
+int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, int* P, int* pc_id);
+int pcs_release(pcs_handle* h, int pc_id);
+/* One step: host in/out [n_channels][buffer_size] (pinned for asynchrony);
+ * returns after enqueueing; pcs_query / pcs_sync observe completion. */
+int pcs_step(pcs_handle* h, const float* in, float* out, int n_channels);
+int pcs_query(pcs_handle* h);
+int pcs_sync(pcs_handle* h);
+long long pcs_bytes_in_use(const pcs_handle* h);
+int pcs_live(const pcs_handle* h);
+long long pcs_kernel_launches(const pcs_handle* h);
+const char* pcs_last_error(const pcs_handle* h);
+void pcs_destroy(pcs_handle* h);
+
 /* Size of the static device scratch array used by pc_convolve_noalloc. */
 #define PC_NOALLOC_SCRATCH_BYTES (32 << 20)
 

@@ -106,6 +106,17 @@ SIGNATURES = {
     "pcd_destroy": (None, [C.c_void_p]),
     "pcd_last_error": (C.c_char_p, [C.c_void_p]),
     "pcd_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "pcs_create": (C.c_void_p, [C.c_int, C.c_longlong, C.c_int]),
+    "pcs_admit": (C.c_int, [C.c_void_p, _f32p, C.c_int, C.c_int, _i32p, _i32p, C.POINTER(C.c_int)]),
+    "pcs_release": (C.c_int, [C.c_void_p, C.c_int]),
+    "pcs_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "pcs_query": (C.c_int, [C.c_void_p]),
+    "pcs_sync": (C.c_int, [C.c_void_p]),
+    "pcs_bytes_in_use": (C.c_longlong, [C.c_void_p]),
+    "pcs_live": (C.c_int, [C.c_void_p]),
+    "pcs_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "pcs_last_error": (C.c_char_p, [C.c_void_p]),
+    "pcs_destroy": (None, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -61,8 +61,9 @@ struct Task {
     int T, s_blocks, cs, rmask;
     int k0, k1, M, in_ch;
     int out_ch, mix_mode, zero_outs, zero_off;
-    int rin_mask, lv_index, p_lo, pad0;   // p_lo: first part summed by a spread task
-    float scale, pad1, pad2, pad3;
+    int rin_mask, lv_index, p_lo, active;   // p_lo: first part summed by a spread task
+    float scale, pad1;
+    long long origin;   // step at which this PC's time starts (0 for a static bank)
     float2* H;
     float2* X;
     float2* Yp;
@@ -73,6 +74,13 @@ struct Task {
     int emask[kEmitLevels];
 };
 static_assert(sizeof(Task) == 192, "Task record is loaded as 12 x 16 bytes");
+
+// One CTA of a serving pool's step: descriptor slot and sub-task (0: the
+// level's fire, s >= 1: the s-th bin tile of its spread slice).
+struct PoolCta {
+    int slot;
+    int sub;
+};
 
 // Where step c's input/output live: base + (c - step0) * step_stride +
 // sample * sample_stride + channel * ch_stride.

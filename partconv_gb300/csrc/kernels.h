@@ -31,6 +31,8 @@ cudaError_t prepare_kernels();
 // be a step kernel of the same handle (or nothing)
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
                               const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl);
+cudaError_t launch_pool_class(int cls, int grid, int maxN, const Bank& bank, const Task* slots, const PoolCta* map,
+                              const RunState& rs, cudaStream_t st);
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,
                            cudaStream_t st);
 cudaError_t launch_set_state(RunState* dst, const RunState& v, cudaStream_t st);

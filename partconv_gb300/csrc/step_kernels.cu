@@ -94,6 +94,7 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
     const bool active = k < tk.k1;
     long long bt;      // block whose partial sum this step builds
     float2* dst;
+    c -= tk.origin;    // the PC's own step count
     if (tk.T == 1) {   // level 0: parts p >= 2 of block c + 1
         bt = c + 1;
         dst = tk.Yp + (size_t)(bt & 1) * tk.cs;
@@ -158,12 +159,13 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     float* emit = reinterpret_cast<float*>(h0s + (N + 2));   // N0 floats (PREFETCH, level 0)
     const Twiddles tw{twt, logN};
 
+    const long long io_step = c - rs.io.step0;   // I/O is addressed by the global step
+    c -= tk.origin;                              // schedule and rings by the PC's own steps
     const long long q = c + 1 + tk.s_blocks;
     const long long b = q / tk.T - 1;
     const int slot = (int)imod(b, P);
     const long long t_new = c * (long long)N0;
     const long long t_end = t_new + N0;
-    const long long io_step = c - rs.io.step0;
     const float* in = rs.io.in + io_step * rs.io.in_step + (long long)tk.in_ch * rs.io.in_ch;
     const long long isamp = rs.io.in_sample;
     const float scale = tk.scale;
@@ -457,6 +459,76 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
 }
 
 // ---------------------------------------------------------------------------
+// Serving pool: PCs join and leave between steps, so instead of per-phase
+// task lists every CTA maps to one (descriptor, sub-task) pair of a map that
+// changes only on admission or release.  Sub-task 0 fires the descriptor's
+// level when its block completes at this step; sub-task s >= 1 is the s-th
+// bin tile of the level's spread slice for this step (level 0: all bins,
+// parts >= 2; level L: slice (phase - 1) of T_L - 1, parts >= 1).  Tiles or
+// fires with nothing to do this step return at once.
+// ---------------------------------------------------------------------------
+template <class C>
+__global__ void __launch_bounds__(C::NT) pool_kernel(Bank bank, const Task* __restrict__ slots,
+                                                     const PoolCta* __restrict__ map, RunState rs_val) {
+    extern __shared__ float4 dyn_smem[];
+    __shared__ __align__(16) Task tk;
+    __shared__ __align__(16) RunState rs;
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    const PoolCta pm = map[blockIdx.x];
+    if (tid < 12) reinterpret_cast<int4*>(&tk)[tid] = __ldg(reinterpret_cast<const int4*>(slots + pm.slot) + tid);
+    if (tid == 64) rs = rs_val;
+    __syncthreads();
+    const long long c = rs.step_base;
+    const long long cl = c - tk.origin;   // the PC's own step count
+    if (!tk.active || cl < 0) return;
+    const long long q = cl + 1 + tk.s_blocks;
+    if (pm.sub == 0) {
+        if (q % tk.T != 0) return;
+        fire_body<C>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
+        return;
+    }
+    int lo, hi, p_lo;
+    if (tk.T == 1) {
+        if (tk.P < 3) return;
+        lo = 0;
+        hi = tk.cs;
+        p_lo = 2;
+    } else {
+        if (tk.P < 2) return;
+        const int phi = (int)(q % tk.T);
+        if (phi == 0) return;
+        const int j = phi - 1, nch = tk.T - 1;
+        lo = (int)(((long long)j * tk.cs / nch) & ~1LL);
+        hi = (j == nch - 1) ? tk.cs : (int)(((long long)(j + 1) * tk.cs / nch) & ~1LL);
+        p_lo = 1;
+    }
+    const int k0 = lo + (pm.sub - 1) * (2 * kSpreadLanes);
+    if (k0 >= hi) return;
+    __syncthreads();   // everyone has read the fire form of the record
+    if (tid == 0) {
+        tk.kind = 1;
+        tk.k0 = k0;
+        tk.k1 = min(hi, k0 + 2 * kSpreadLanes);
+        tk.p_lo = p_lo;
+    }
+    __syncthreads();
+    spread_body<C::NT>(tk, c, dyn_smem);
+}
+
+cudaError_t launch_pool_class(int cls, int grid, int maxN, const Bank& bank, const Task* slots, const PoolCta* map,
+                              const RunState& rs, cudaStream_t st) {
+    if (grid <= 0) return cudaSuccess;
+    const size_t smem = class_smem_bytes(cls, maxN);
+    switch (cls) {
+        case 0: pool_kernel<Cls0><<<grid, Cls0::NT, smem, st>>>(bank, slots, map, rs); break;
+        case 1: pool_kernel<Cls1><<<grid, Cls1::NT, smem, st>>>(bank, slots, map, rs); break;
+        default: pool_kernel<Cls2><<<grid, Cls2::NT, smem, st>>>(bank, slots, map, rs); break;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Filter spectra: H = rfft([0_N, h_row]) / 2N for one row per CTA.
 // ---------------------------------------------------------------------------
 template <int NT, int MAXB>
@@ -524,6 +596,15 @@ cudaError_t prepare_kernels() {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(spectra_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(12 * 16384));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(pool_kernel<Cls0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)class_smem_bytes(0, Cls0::MAXN));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(pool_kernel<Cls1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)class_smem_bytes(1, Cls1::MAXN));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(pool_kernel<Cls2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)class_smem_bytes(2, Cls2::MAXN));
     return e;
 }
 

@@ -20,7 +20,7 @@ HEADER = os.path.join(ROOT, "include", "partconv_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(pc[fmd]?_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(pc[fmds]?_[a-z_]+)\s*\(", text)))
 
 
 def test_header_declares_the_abi():

@@ -48,7 +48,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0, help="base steps for the per-kernel profile (0: 4*H)")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3"],
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"],
                     help="cfg2: batched streams (the headline); cfg3: 64x64 MIMO")
     return ap.parse_args()
 
@@ -472,12 +472,90 @@ def run_mimo(args):
     return 0
 
 
+def run_adjoint(args):
+    """Config 4: batch 8 x 2^18, learnable 2^16-tap IR, MSE loss; a step is
+    forward + hand-written backward (dL/dx and dL/dh)."""
+    import torch
+
+    from partconv_gb300 import workloads as wl
+    from partconv_gb300.adjoint import PartitionedConv
+
+    torch.cuda.set_device(0)
+    c = wl.cfg4()
+    x = torch.from_numpy(c["x"]).cuda().requires_grad_(True)
+    B, T = c["x"].shape
+    target = torch.from_numpy(np.stack([wl.conv_fp64(c["x"][b], c["h_target"], T) for b in range(B)])
+                              .astype(np.float32)).cuda()
+    mod = PartitionedConv(c["h_init"], c["N"], c["P"], B, T).cuda()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        mod.h.grad = None
+        x.grad = None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        loss = torch.mean((mod(x) - target) ** 2)
+        loss.backward()
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = mod.plan.kernel_launches()
+    evs = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    audio = B * T / FS
+    print(json.dumps({"metric": "audio-s/s (differentiable conv, forward + backward)", "value": audio / (ms / 1e3),
+                      "unit": "audio-s/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+                      "data": "synthetic (seeded numpy PCG64, cfg seed 1004)",
+                      "config": {"workload": "cfg4: batch 8 x 2^18, IR 2^16 taps, layout 512x8|4096x15, MSE"},
+                      "gpu_launches": int(mod.plan.kernel_launches() - l0)}))
+    return 0
+
+
+def run_serving(args):
+    """Config 5: Poisson arrivals at 200/s up to 1000 concurrent streams of
+    1/2/8 channels, IRs 2^12..2^20 taps, base blocks 64..1024, 10 s of audio
+    each, real time; per-block latency and deadline misses."""
+    import torch
+
+    from partconv_gb300 import workloads as wl
+    from partconv_gb300.serving import Server
+
+    torch.cuda.set_device(0)
+    reqs = wl.cfg5_requests(n_streams=args.streams if args.streams != 32 else 1000)
+    t0 = time.time()
+    irs = []
+    for r in reqs:
+        g = np.random.Generator(np.random.PCG64(r["seed"]))
+        irs.append([wl.decaying_ir(g, r["ir_len"], r["t60"]) for _ in range(r["channels"])])
+    noise = (0.1 * np.random.default_rng(5).standard_normal(1 << 22)).astype(np.float32)
+    gen_s = time.time() - t0
+    srv = Server(hbm_budget_bytes=160 << 30, max_pcs_per_pool=4096)
+    stats = srv.run_load(reqs, irs, noise, max_concurrent=1000, max_seconds=120.0)
+    print(json.dumps({"metric": "serving: per-block latency and audio-s/s (cfg5 mix, real time)",
+                      "value": stats["audio_s_per_s"], "unit": "audio-s/s", "n_gpus": 1, "higher_is_better": True,
+                      "dtype": "f32", "data": "synthetic (seeded; inputs are slices of one noise buffer)",
+                      "config": {"workload": "cfg5: 1000 streams, Poisson 200/s, 1/2/8 ch, IR 2^12..2^20, "
+                                             "N0 64..1024, 10 s each", "request_gen_s": gen_s},
+                      "serving": stats}))
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "cfg3":
         return run_mimo(args)
+    if args.workload == "cfg4":
+        return run_adjoint(args)
+    if args.workload == "cfg5":
+        return run_serving(args)
     return run_ours(args)
 
 

@@ -261,3 +261,114 @@ class Server:
                          deadline_miss_rate=miss / len(lat_us))
         outputs = {r.rid: r.y for r in finished} if keep_outputs else None
         return stats, outputs
+
+    def run_load(self, requests, irs, noise: np.ndarray, max_concurrent: int = 1000, max_seconds: float = 120.0):
+        """Real-time load run for throughput and latency: like ``run`` but
+        every channel reads its input from ``noise`` (a shared float32 buffer,
+        channel c of request r starting at a seeded offset), outputs are
+        discarded, and per-tick gathers are vectorised so the host keeps up
+        with thousands of channels.  irs[r] holds request r's IRs."""
+        order = sorted(range(len(requests)), key=lambda i: requests[i]["arrival"])
+        rng = np.random.default_rng(4321)
+        pend = list(order)
+        queue = []
+        pools = self.pools
+        period = {b: b / self.fs for b in pools}
+        st = {b: dict(pid=np.zeros(0, np.int64), off=np.zeros(0, np.int64), pos=np.zeros(0, np.int64),
+                      left=np.zeros(0, np.int64), req=np.zeros(0, np.int64)) for b in pools}
+        pcs_of = {}
+        next_tick = {b: 0.0 for b in pools}
+        inflight = {b: None for b in pools}
+        lat_us, lat_w, miss_w, blocks = [], [], 0, 0
+        concurrent = peak = finished = 0
+        audio = 0.0
+        nz = len(noise)
+        t0 = time.perf_counter()
+        while finished < len(requests):
+            t = time.perf_counter() - t0
+            if t > max_seconds:
+                break
+            while pend and requests[pend[0]]["arrival"] <= t:
+                queue.append(pend.pop(0))
+            while queue and concurrent < max_concurrent:
+                ri = queue[0]
+                spec = requests[ri]
+                b = spec["N0"]
+                N, P = serving_layout(spec["ir_len"], b)
+                got = []
+                ok = True
+                for ch in range(spec["channels"]):
+                    try:
+                        got.append(pools[b].admit(irs[ri][ch], N, P))
+                    except PartConvError as e:
+                        if e.code not in (nat.PC_ERR_NOMEM, nat.PC_ERR_LIMIT):
+                            raise
+                        ok = False
+                        break
+                if not ok:
+                    for pid in got:
+                        pools[b].release(pid)
+                    break
+                queue.pop(0)
+                nblk = spec["frames"] // b
+                s = st[b]
+                k = len(got)
+                s["pid"] = np.concatenate([s["pid"], np.array(got, np.int64)])
+                s["off"] = np.concatenate([s["off"], rng.integers(0, nz - spec["frames"], k)])
+                s["pos"] = np.concatenate([s["pos"], np.zeros(k, np.int64)])
+                s["left"] = np.concatenate([s["left"], np.full(k, nblk, np.int64)])
+                s["req"] = np.concatenate([s["req"], np.full(k, ri, np.int64)])
+                pcs_of[ri] = got
+                concurrent += 1
+                peak = max(peak, concurrent)
+            progressed = False
+            for b, pool in pools.items():
+                s = st[b]
+                if inflight[b] is not None and pool.done():
+                    tick_t, nmem = inflight[b]
+                    lat = (time.perf_counter() - t0 - tick_t) * 1e6
+                    lat_us.append(lat)
+                    lat_w.append(nmem)
+                    if lat > period[b] * 1e6:
+                        miss_w += nmem
+                    blocks += nmem
+                    inflight[b] = None
+                    progressed = True
+                    # channels whose last block just completed leave the pool
+                    done = s["left"] == 0
+                    if done.any():
+                        for ri in np.unique(s["req"][done]):
+                            for pid in pcs_of.pop(int(ri)):
+                                pool.release(pid)
+                            finished += 1
+                            concurrent -= 1
+                            audio += requests[int(ri)]["channels"] * requests[int(ri)]["frames"] / self.fs
+                        keep = ~done
+                        for key in s:
+                            s[key] = s[key][keep]
+                if inflight[b] is None and len(s["pid"]) and next_tick[b] <= t:
+                    idx = s["off"] + s["pos"] * b
+                    self._in[b].numpy()[s["pid"]] = noise[idx[:, None] + np.arange(b)]
+                    s["pos"] += 1
+                    s["left"] -= 1
+                    tick_t = time.perf_counter() - t0
+                    if next_tick[b] < tick_t - period[b]:
+                        next_tick[b] = tick_t
+                    next_tick[b] += period[b]
+                    pool.step(self._in[b].data_ptr(), self._out[b].data_ptr(), int(s["pid"].max()) + 1)
+                    inflight[b] = (tick_t, len(s["pid"]))
+                    progressed = True
+            if not progressed:
+                time.sleep(20e-6)
+        wall = time.perf_counter() - t0
+        lat = np.array(lat_us)
+        w = np.array(lat_w, np.float64)
+        order_l = np.argsort(lat)
+        cw = np.cumsum(w[order_l]) / max(w.sum(), 1.0)
+        pct = lambda q: float(lat[order_l][min(np.searchsorted(cw, q), len(lat) - 1)]) if len(lat) else None  # noqa: E731
+        return {"requests": len(requests), "finished": finished, "peak_concurrent": peak, "wall_s": wall,
+                "audio_s": audio, "audio_s_per_s": audio / wall if wall > 0 else 0.0, "blocks": blocks,
+                "latency_us_p50": pct(0.50), "latency_us_p99": pct(0.99),
+                "latency_us_max": float(lat.max()) if len(lat) else None,
+                "deadline_miss_rate": miss_w / max(blocks, 1),
+                "launches": sum(p.kernel_launches() for p in pools.values())}

@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0, help="base steps for the per-kernel profile (0: 4*H)")
+    ap.add_argument("--layouts", default="auto", choices=["auto", "chain"],
+                    help="cfg2 layouts: measured-GPU autotuner (cached) or the minimum-slack chain")
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"],
                     help="cfg2: batched streams (the headline); cfg3: 64x64 MIMO")
     return ap.parse_args()
@@ -131,10 +133,21 @@ def ncu_traffic():
 
 
 # --------------------------------------------------------------------------
-def workload(streams: int, samples: int):
+def workload(streams: int, samples: int, layouts: str = "auto", measure: bool = True):
+    """Config 2 inputs.  layouts: "auto" = the measured-GPU autotuner's
+    choice per IR length class (its cache, measuring on a miss when allowed;
+    the minimum-slack chain when not), "chain" = the minimum-slack chain."""
+    from partconv_gb300 import autotune
     from partconv_gb300 import workloads as wl
 
-    c = wl.cfg2(n_streams=streams, n_samples=samples)
+    def pick(L, n0):
+        if layouts == "auto":
+            got = autotune.choose_layout(L, n0, batch=streams) if measure else autotune.cached_layout(L, n0, streams)
+            if got:
+                return got
+        return wl.chain_layout(L, n0)
+
+    c = wl.cfg2(n_streams=streams, n_samples=samples, layout_fn=pick)
     N0 = c["N0"]
     tail = max(len(h) for h in c["irs"])
     frames = samples + (tail + N0 - 1) // N0 * N0
@@ -171,7 +184,7 @@ def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
         return 0
-    c, x, frames = workload(args.streams, args.samples)
+    c, x, frames = workload(args.streams, args.samples, args.layouts, measure=False)
     import oracle
 
     threads = os.cpu_count() or 1
@@ -218,7 +231,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    c, x_host, frames = workload(args.streams, args.samples)
+    c, x_host, frames = workload(args.streams, args.samples, args.layouts)
     S, N0 = x_host.shape[0], c["N0"]
     pcs = [dict(ir=h, N=N, P=P, in_ch=s, out_ch=s) for s, (h, (N, P)) in enumerate(zip(c["irs"], c["layouts"]))]
     m = PartConvMulti()
@@ -369,7 +382,9 @@ def run_ours(args):
             "dtype": "f32", "data": "synthetic (seeded numpy PCG64, cfg seed 1002)",
             "config": {"workload": f"cfg2: {S} streams x {args.samples} samples + IR flush ({frames} per stream), "
                                    f"IR 2^14..2^19 taps, N0={N0}, one handle, graph-replayed base steps",
-                       "layouts": "minimum-slack level chain (ratio 8, max block 16384)",
+                       "layouts": ("autotuned from measured GPU timings (partconv_gb300/autotune_cache.json)"
+                                   if args.layouts == "auto" else "minimum-slack level chain (ratio 8, max 16384)"),
+                       "layout_set": sorted({f"{N}x{P}" for N, P in c["layouts"]})[:8],
                        "streams": S, "frames_per_stream": frames, "N0": N0,
                        "hyperperiod_steps": info.hyperperiod,
                        "l2": "256 MB buffer written between timed steps (outside the events); "

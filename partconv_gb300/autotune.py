@@ -1,0 +1,163 @@
+"""Partition-layout autotuner from measured GPU timings.
+
+The reference picks layouts offline: src/tune.py:91-154 benches candidate
+layouts through PartConvFilter.bench on the CPU, and matlab/optimal_part.m
+searches a cost model (4k log2(2N) + 4 per block).  Here candidates are
+timed on the GPU engine itself: each candidate layout runs a batch of
+identical streams (the way the batched engine will run it) for a few
+hyperperiods of base steps, and the layout with the lowest time per
+stream-step wins.  Results are cached per (IR length class, base block,
+batch class, GPU) in a JSON file, the analogue of the reference's FFTW
+wisdom file (src/partconvMulti.cpp:250-254).
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+
+import numpy as np
+
+from . import workloads as wl
+
+DEFAULT_CACHE = os.environ.get("PARTCONV_AUTOTUNE_CACHE") or os.path.join(
+    os.path.dirname(os.path.abspath(__file__)), "autotune_cache.json")
+_lock = threading.Lock()
+
+
+def candidate_layouts(ir_len: int, N0: int, max_block: int = 16384):
+    """Minimum-slack chains: ratios 2, 4 and 8, largest blocks up to
+    max_block, plus the one-level uniform layout for short IRs."""
+    seen, out = set(), []
+    for ratio in (2, 4, 8):
+        mb = N0
+        while mb * ratio <= max_block:
+            mb *= ratio
+        tops = []
+        while mb >= N0 * ratio:
+            tops.append(mb)
+            mb //= ratio
+        for top in tops[:3]:
+            N, P = wl.chain_layout(ir_len, N0, ratio=ratio, max_block=top)
+            key = (tuple(N), tuple(P))
+            if key not in seen and len(N) <= 16:
+                seen.add(key)
+                out.append((list(N), list(P)))
+    if ir_len <= 64 * N0:
+        N, P = [N0], [-(-ir_len // N0)]
+        if (tuple(N), tuple(P)) not in seen:
+            out.append((N, P))
+    return out
+
+
+def _gpu_name():
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_name(0)
+    except Exception:
+        pass
+    return "unknown"
+
+
+def _len_class(ir_len: int) -> int:
+    return 1 << int(np.ceil(np.log2(max(ir_len, 2))))
+
+
+def measure_layout(N, P, ir_len: int, batch: int = 32, steps: int = 0, seed: int = 0) -> float:
+    """Device time (µs) per base step of `batch` streams of this layout."""
+    import torch
+
+    from .multi import PartConvMulti
+    from . import PC_PLANAR
+
+    rng = np.random.default_rng(seed)
+    N0 = N[0]
+    pcs = [dict(ir=wl.decaying_ir(rng, ir_len, 1.0), N=N, P=P, in_ch=s, out_ch=s) for s in range(batch)]
+    m = PartConvMulti()
+    m.setup_layout(48000, N0, batch, batch, pcs)
+    H = m.info().hyperperiod
+    nsteps = steps or max(2 * H, 128)
+    nsteps = (nsteps + H - 1) // H * H
+    x = torch.randn(batch, nsteps * N0, device="cuda") * 0.1
+    y = torch.empty_like(x)
+    m.process_device(y, x, nsteps * N0, PC_PLANAR)   # warm
+    torch.cuda.synchronize()
+    m.reset()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    m.process_device(y, x, nsteps * N0, PC_PLANAR)
+    e1.record()
+    torch.cuda.synchronize()
+    us = e0.elapsed_time(e1) * 1e3 / nsteps
+    m.cleanup()
+    return us
+
+
+def _load(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _fit(N, P, ir_len):
+    """Fit a level structure chosen for a length class to the exact length."""
+    N, P = list(N), list(P)
+    s = sum(n * p for n, p in zip(N[:-1], P[:-1]))
+    while len(N) > 1 and s >= ir_len:
+        N.pop()
+        P.pop()
+        s = sum(n * p for n, p in zip(N[:-1], P[:-1]))
+    P[-1] = max(1, -(-(ir_len - s) // N[-1]))
+    return N, P
+
+
+def _key(ir_len, N0, batch, gpu=None):
+    lc = _len_class(ir_len)
+    bc = 1 << int(np.ceil(np.log2(max(batch, 1))))
+    return f"{gpu or _gpu_name()}|N0={N0}|len={lc}|batch={bc}", lc, bc
+
+
+def cached_layout(ir_len: int, N0: int, batch: int = 32, cache: str | None = DEFAULT_CACHE):
+    """The cached choice for this key without measuring (None on a miss).
+    Without a GPU (or with no entry for this one) an entry of the same
+    length, block and batch class measured on another GPU is taken."""
+    if not cache:
+        return None
+    db = _load(cache)
+    key, _, _ = _key(ir_len, N0, batch)
+    rec = db.get(key)
+    if rec is None:
+        tail = key[key.index("|"):]
+        rec = next((v for k, v in sorted(db.items()) if k.endswith(tail)), None)
+    return _fit(rec["best"]["N"], rec["best"]["P"], ir_len) if rec else None
+
+
+def choose_layout(ir_len: int, N0: int, batch: int = 32, cache: str | None = DEFAULT_CACHE, verbose: bool = False):
+    """Layout (N, P) with the lowest measured time per step for IRs of this
+    length class; P[-1] is recomputed for the exact ir_len."""
+    key, lc, bc = _key(ir_len, N0, batch)
+    with _lock:
+        db = _load(cache) if cache else {}
+    if key not in db:
+        results = []
+        for N, P in candidate_layouts(lc, N0):
+            us = measure_layout(N, P, lc, batch=bc)
+            results.append({"N": N, "P": P, "us_per_step": us})
+            if verbose:
+                print(f"  {N} {P}: {us:.2f} us/step")
+        best = min(results, key=lambda r: r["us_per_step"])
+        db[key] = {"best": best, "candidates": results}
+        if cache:
+            with _lock:
+                cur = _load(cache)
+                cur[key] = db[key]
+                tmp = cache + ".tmp"
+                with open(tmp, "w") as f:
+                    json.dump(cur, f, indent=1, sort_keys=True)
+                os.replace(tmp, cache)
+    return _fit(db[key]["best"]["N"], db[key]["best"]["P"], ir_len)

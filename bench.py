@@ -39,11 +39,12 @@ FS = 48000
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--streams", type=int, default=32)
-    ap.add_argument("--samples", type=int, default=1 << 19)
+    ap.add_argument("--samples", type=int, default=None,
+                    help="input samples per stream/channel (default: the workload's, 2^19 cfg2, 2^18 cfg3)")
     ap.add_argument("--plain-blocks", type=int, default=96, help="pc_run calls per stream in the plain sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
@@ -429,7 +430,7 @@ def run_mimo(args):
     from partconv_gb300.mimo import PartConvMIMO
 
     torch.cuda.set_device(0)
-    c = wl.cfg3()
+    c = wl.cfg3(n_samples=args.samples or (1 << 18))
     irs, N, P = c["irs"], c["N"], c["P"]
     n_in, n_out, L = irs.shape
     frames = c["x"].shape[1] + L
@@ -563,6 +564,8 @@ def run_serving(args):
 
 def main():
     args = parse_args()
+    if args.samples is None and args.workload == "cfg2":
+        args.samples = 1 << 19
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "cfg3":

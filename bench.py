@@ -4,7 +4,8 @@
 Workload (one "step"): 32 independent mono float32 streams, each 2^19
 samples of N(0, 0.1^2) input followed by zeros to flush its IR (IR lengths
 log-uniform in [2^14, 2^19] taps, T60 U(0.3, 4) s, seeded), base block 256,
-layouts from the minimum-slack level chain, all streams in one handle: every
+layouts chosen by the measured-GPU autotuner (partconv_gb300/autotune.py,
+cached in partconv_gb300/autotune_cache.json), all streams in one handle: every
 256-sample base block is one launch per kernel class, replayed from CUDA
 graphs.  A step starts from reset state and processes the whole workload.
 
@@ -62,6 +63,26 @@ def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def max_over_ranks(values, device=None):
+    """Element-wise maximum over ranks of per-rank timings: a replicated job
+    takes as long as its slowest rank.  Identity without a process group."""
+    import torch
+    import torch.distributed as dist
+
+    vals = [float(v) for v in values]
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return vals
+    t = torch.tensor(vals, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def job_rate(world_size: int, units_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput of independent replicas: all ranks' units over
+    the slowest rank's time."""
+    return world_size * units_per_rank / seconds
 
 
 class ClockSampler:
@@ -284,12 +305,8 @@ def run_ours(args):
     wall = time.perf_counter() - w0
     clk = clocks.stop()
     launches = m.kernel_launches() - launches0
-    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * audio_s / (ms / 1e3)
+    ms = max_over_ranks([np.mean([a.elapsed_time(b) for a, b in evs])], dev)[0]
+    value = job_rate(ws, audio_s, ms / 1e3)
 
     # ---- e2e: host buffers through the C ABI (pinned), copies timed -------------
     xp = torch.from_numpy(x_host).pin_memory()
@@ -302,7 +319,9 @@ def run_ours(args):
         t0 = time.perf_counter()
         m.process_into(yp.data_ptr(), xp.data_ptr(), frames, PC_PLANAR)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_v = ws * audio_s / float(np.mean(e2e_times))
+    if ws > 1:
+        torch.distributed.barrier()
+    e2e_v = job_rate(ws, audio_s, max_over_ranks([np.mean(e2e_times)], dev)[0])
     nbytes = x_host.nbytes
 
     # ---- per-kernel profile for the roofline --------------------------------------

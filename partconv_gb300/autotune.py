@@ -26,23 +26,26 @@ _lock = threading.Lock()
 
 
 def candidate_layouts(ir_len: int, N0: int, max_block: int = 16384):
-    """Minimum-slack chains: ratios 2, 4 and 8, largest blocks up to
-    max_block, plus the one-level uniform layout for short IRs."""
+    """Level chains with ratios 2, 4 and 8 and largest blocks up to
+    max_block, each with minimum slack (every level fires within its step)
+    and with the reference's strict slack (larger levels' fires run beside
+    later steps), plus the one-level uniform layout for short IRs."""
     seen, out = set(), []
-    for ratio in (2, 4, 8):
-        mb = N0
-        while mb * ratio <= max_block:
-            mb *= ratio
-        tops = []
-        while mb >= N0 * ratio:
-            tops.append(mb)
-            mb //= ratio
-        for top in tops[:3]:
-            N, P = wl.chain_layout(ir_len, N0, ratio=ratio, max_block=top)
-            key = (tuple(N), tuple(P))
-            if key not in seen and len(N) <= 16:
-                seen.add(key)
-                out.append((list(N), list(P)))
+    for strict in (False, True):
+        for ratio in (2, 4, 8):
+            mb = N0
+            while mb * ratio <= max_block:
+                mb *= ratio
+            tops = []
+            while mb >= N0 * ratio:
+                tops.append(mb)
+                mb //= ratio
+            for top in tops[:3]:
+                N, P = wl.chain_layout(ir_len, N0, ratio=ratio, max_block=top, strict=strict)
+                key = (tuple(N), tuple(P))
+                if key not in seen and len(N) <= 16:
+                    seen.add(key)
+                    out.append((list(N), list(P)))
     if ir_len <= 64 * N0:
         N, P = [N0], [-(-ir_len // N0)]
         if (tuple(N), tuple(P)) not in seen:

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -131,6 +133,7 @@ struct pc_handle {
     int device = -1;
     cudaStream_t stream = nullptr;
     cudaStream_t side[kClasses] = {nullptr, nullptr, nullptr};   // graph-capture branches
+    cudaStream_t aside[kClasses] = {nullptr, nullptr, nullptr};  // deferred fires (graph capture)
 
     int fs = 0, N0 = 0, n_in = 0, n_out = 0;
     int relaxed = 0;
@@ -153,6 +156,15 @@ struct pc_handle {
     Task* d_tasks = nullptr;
     std::vector<int> off[kClasses], cnt[kClasses];
     std::vector<double> alg_bytes[kClasses];
+    // Deferred fires (levels >= 1 whose output is due more than one step
+    // after their block completes): launched after the step that completed
+    // the block, on a low-priority stream, and joined `due` steps later.
+    struct DGroup {
+        int cls, phase, due, off, cnt;
+        double bytes;
+    };
+    std::vector<DGroup> dgroups;
+    std::vector<std::vector<int>> dg_of_phase;   // phase -> indices into dgroups
     int class_maxN[kClasses] = {0, 0, 0};
     RunState* d_rs = nullptr;
 
@@ -207,6 +219,10 @@ void free_device(pc_handle* h) {
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
+    for (auto& s : h->aside) {
+        if (s) cudaStreamDestroy(s);
+        s = nullptr;
+    }
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     h->ready = false;
@@ -229,6 +245,16 @@ int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool f
         first = false;
         h->launches += 1;
     }
+    // deferred fires of blocks completed by this step, in stream order (a
+    // direct step does not overlap them with later steps)
+    for (int gi : h->dg_of_phase[ph]) {
+        const pc_handle::DGroup& gr = h->dgroups[gi];
+        CK(launch_step_class(gr.cls, gr.cnt, h->class_maxN[gr.cls], h->bank, h->d_tasks + gr.off, rs, nullptr, 0, st,
+                             !first),
+           "deferred fire launch");
+        first = false;
+        h->launches += 1;
+    }
     return PC_OK;
 }
 
@@ -247,8 +273,22 @@ int build_graph(pc_handle* h) {
     if (e != cudaSuccess) return cuda_fail(h, e, "begin capture");
     RunState dummy{};
     long long kernels = 0;
+    struct Pending {
+        int due_step;
+        cudaEvent_t done;
+    };
+    std::vector<Pending> pending;   // deferred fires in flight
     for (int s = 0; s < h->G && e == cudaSuccess; ++s) {
         const int ph = s & (h->H - 1);
+        // deferred fires whose output this step emits join the chain here
+        for (size_t i = 0; i < pending.size() && e == cudaSuccess;) {
+            if (pending[i].due_step <= s) {
+                e = cudaStreamWaitEvent(h->stream, pending[i].done, 0);
+                pending.erase(pending.begin() + i);
+            } else {
+                ++i;
+            }
+        }
         std::vector<cudaEvent_t> joins;
         for (int cls = 0; cls < kClasses && e == cudaSuccess; ++cls) {
             if (cls == h->l0_class || h->cnt[cls][ph] <= 0) continue;
@@ -266,11 +306,31 @@ int build_graph(pc_handle* h) {
         const int c0 = h->l0_class;
         if (e == cudaSuccess)
             e = launch_step_class(c0, h->cnt[c0][ph], h->class_maxN[c0], h->bank, h->d_tasks + h->off[c0][ph], dummy,
-                                  h->d_rs, s, h->stream, s > 0);
+                                  h->d_rs, s, h->stream, s > 0, 1);
         ++kernels;
         for (auto j : joins)
             if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, j, 0);
+        // fires of blocks this step completed: forked after the step, low
+        // priority, joined before the step that first emits their output
+        for (int gi : h->dg_of_phase[ph]) {
+            if (e != cudaSuccess) break;
+            const pc_handle::DGroup& gr = h->dgroups[gi];
+            cudaEvent_t fork = mk();
+            e = cudaEventRecord(fork, h->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->aside[gr.cls], fork, 0);
+            if (e == cudaSuccess)
+                e = launch_step_class(gr.cls, gr.cnt, h->class_maxN[gr.cls], h->bank, h->d_tasks + gr.off, dummy,
+                                      h->d_rs, s, h->aside[gr.cls], false, -1);
+            cudaEvent_t done = mk();
+            if (e == cudaSuccess) e = cudaEventRecord(done, h->aside[gr.cls]);
+            pending.push_back({s + gr.due, done});
+            ++kernels;
+        }
     }
+    // the graph ends with every deferred fire joined (a replay must not
+    // overlap the next one's state update)
+    for (auto& pd : pending)
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, pd.done, 0);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     for (auto ev : evs) cudaEventDestroy(ev);
     if (e == cudaSuccess) e = e2;
@@ -300,8 +360,11 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     int dev = 0;
     CK(cudaGetDevice(&dev), "cudaGetDevice");
     h->device = dev;
-    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream create");
-    for (auto& s : h->side) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream create");
+    int prio_least = 0, prio_greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest), "priority range");
+    CK(cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_greatest), "stream create");
+    for (auto& s : h->side) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_greatest), "stream create");
+    for (auto& s : h->aside) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_least), "stream create");
     CK(prepare_kernels(), "kernel attributes");
 
     h->fs = fs;
@@ -359,11 +422,34 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         std::vector<size_t> xring, pcout, X, Yp, yr;
         size_t mix = 0, carry = 0;
     } so;
-    std::vector<int> rin(npc), rl(nlv);
-    for (int i = 0; i < npc; ++i) {
-        long r = 1;
-        while (r < 2L * h->specs[i].N.back()) r <<= 1;
-        rin[i] = (int)r;
+    // Deferral window of each level (0: fires within its step).  Level L's
+    // first output sample of a block is due slack = (s_L - N_L)/N0 steps
+    // after the step that completes the block; the fire is deferred by
+    // w = min(slack, T - 2) steps so that it is joined before the level's
+    // next block completes (the spreads of the block after next read its
+    // spectrum).  Its window stays in the input ring meanwhile.
+    std::vector<int> rin(npc), rl(nlv), dwin(nlv, 0);
+    {
+        int li = 0;
+        for (int i = 0; i < npc; ++i) {
+            const PCSpec& p = h->specs[i];
+            long need = 2L * p.N.back();
+            long sacc = 0;
+            for (size_t L = 0; L < p.N.size(); ++L, ++li) {
+                const long T = p.N[L] / N0, sb = sacc / N0;
+                if (L > 0 && T >= 4) {
+                    const long w = std::min(sb - T, T - 2);
+                    if (w >= 1) {
+                        dwin[li] = (int)w;
+                        need = std::max(need, 2L * p.N[L] + (w + 1) * (long)N0);
+                    }
+                }
+                sacc += (long)p.N[L] * p.P[L];
+            }
+            long r = 1;
+            while (r < need) r <<= 1;
+            rin[i] = (int)r;
+        }
     }
     {
         int li = 0;
@@ -416,6 +502,8 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     // Tasks point into the arena, so they are built after the state offsets
     // are known; first count them to size the table.
     std::vector<std::vector<std::vector<Task>>> lists(kClasses, std::vector<std::vector<Task>>(Hh));
+    std::map<std::tuple<int, int, int>, std::vector<Task>> dlists;   // (phase, due, class) -> deferred fires
+    std::map<std::tuple<int, int, int>, double> dbytes;
     for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(Hh, 0.0);
     // order: larger fires first (longest CTAs start first), then level-0
     // fires, then spread tasks
@@ -446,19 +534,26 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             t.lv_index = li;
             t.scale = d.scale;
             const int cls = fire_class_of(l.N);
-            lists[cls][g].push_back(t);
             // bytes a fire must move: H0 row read, new X row written, the
-            // partial-sum row read (level 0 also X_{b-1} and H_1 rows), the
-            // 2N-sample window read, N samples written; level 0 also reads
-            // the other levels' due slices and appends N0 input samples
+            // partial-sum row read (level 0 and deferred levels also X_{b-1}
+            // and H_1 rows), the 2N-sample window read, N samples written;
+            // level 0 also reads the other levels' due slices and appends N0
+            // input samples
             const double C = l.N + 1.0;
             double b = 8.0 * C * 2.0 + 12.0 * l.N;
-            if (l.T == 1) {
+            if (l.T == 1 || dwin[li] > 0) {
                 b += 8.0 * C * (l.P >= 2 ? 2.0 : 0.0) + (l.P >= 3 ? 8.0 * C : 0.0);
-                b += 4.0 * N0 * (d.M - 1) + 4.0 * N0;
+                if (l.T == 1) b += 4.0 * N0 * (d.M - 1) + 4.0 * N0;
             } else if (l.P >= 2) {
                 b += 8.0 * C;
             }
+            if (dwin[li] > 0) {
+                t.dfer = 1;
+                dlists[std::make_tuple(g, dwin[li] + 1, cls)].push_back(t);
+                dbytes[std::make_tuple(g, dwin[li] + 1, cls)] += b;
+                continue;
+            }
+            lists[cls][g].push_back(t);
             h->alg_bytes[cls][g] += b;
         }
         const int sc = h->l0_class;
@@ -469,6 +564,15 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 if (l.P < 3) continue;
                 lo = 0;
                 hi = l.cs;
+                p_lo = 2;
+            } else if (dwin[li] > 0) {
+                // parts >= 2 of the next deferred fire, in T slices over all
+                // phases (the fire's own step builds the last slice)
+                if (l.P < 3) continue;
+                const int phi = (g + 1 + l.s_blocks) % l.T;
+                const int j = (phi + l.T - 1) % l.T, nch = l.T;
+                lo = (int)(((long)j * l.cs / nch) & ~1L);
+                hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
                 p_lo = 2;
             } else {
                 if (l.P < 2) continue;
@@ -491,6 +595,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 t.k1 = std::min(hi, k0 + spread_task_bins());
                 t.p_lo = p_lo;
                 t.lv_index = li;
+                t.dfer = dwin[li] > 0;
                 lists[sc][g].push_back(t);
             }
             h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0) * (hi - lo);
@@ -506,6 +611,20 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             ntasks += lists[cls][g].size();
         }
         h->off[cls][Hh] = (int)ntasks;
+    }
+    h->dgroups.clear();
+    h->dg_of_phase.assign(Hh, {});
+    for (auto& kv : dlists) {
+        pc_handle::DGroup gr;
+        gr.phase = std::get<0>(kv.first);
+        gr.due = std::get<1>(kv.first);
+        gr.cls = std::get<2>(kv.first);
+        gr.off = (int)ntasks;
+        gr.cnt = (int)kv.second.size();
+        gr.bytes = dbytes[kv.first];
+        h->dg_of_phase[gr.phase].push_back((int)h->dgroups.size());
+        h->dgroups.push_back(gr);
+        ntasks += kv.second.size();
     }
     const size_t off_tasks = cv.take(sizeof(Task) * std::max<size_t>(1, ntasks));
 
@@ -556,9 +675,12 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     }
     std::vector<Task> all_tasks;
     all_tasks.reserve(ntasks);
+    std::vector<const std::vector<Task>*> in_order;
     for (int cls = 0; cls < kClasses; ++cls)
-        for (int g = 0; g < Hh; ++g)
-            for (Task t : lists[cls][g]) {
+        for (int g = 0; g < Hh; ++g) in_order.push_back(&lists[cls][g]);
+    for (auto& kv : dlists) in_order.push_back(&kv.second);
+    for (const auto* lst : in_order)
+            for (Task t : *lst) {
                 const DevLevel& l = h->h_lv[t.lv_index];
                 const DevPC& d = h->h_pcs[l.pc];
                 t.H = l.H;
@@ -1040,6 +1162,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     struct Rec {
         int cls;
         int phase;
+        int dgroup;   // -1: the class's per-phase list
         cudaEvent_t a, b;
     };
     std::vector<Rec> recs;
@@ -1057,11 +1180,25 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
             const int cls = (h->l0_class + k) % kClasses;
             const int n = h->cnt[cls][ph];
             if (n <= 0) continue;
-            Rec r{cls, ph, nullptr, nullptr};
+            Rec r{cls, ph, -1, nullptr, nullptr};
             cudaEventCreate(&r.a);
             cudaEventCreate(&r.b);
             cudaEventRecord(r.a, h->stream);
             cudaError_t e = launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs,
+                                              nullptr, 0, h->stream, false);
+            cudaEventRecord(r.b, h->stream);
+            recs.push_back(r);
+            h->launches += 1;
+            if (e != cudaSuccess) rc = cuda_fail(h, e, "profile launch");
+        }
+        for (int gi : h->dg_of_phase[ph]) {
+            if (rc != PC_OK) break;
+            const pc_handle::DGroup& gr = h->dgroups[gi];
+            Rec r{gr.cls, ph, gi, nullptr, nullptr};
+            cudaEventCreate(&r.a);
+            cudaEventCreate(&r.b);
+            cudaEventRecord(r.a, h->stream);
+            cudaError_t e = launch_step_class(gr.cls, gr.cnt, h->class_maxN[gr.cls], h->bank, h->d_tasks + gr.off, rs,
                                               nullptr, 0, h->stream, false);
             cudaEventRecord(r.b, h->stream);
             recs.push_back(r);
@@ -1077,7 +1214,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
         float t = 0.f;
         if (se == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
             ms[r.cls] += t;
-            bytes[r.cls] += h->alg_bytes[r.cls][r.phase];
+            bytes[r.cls] += r.dgroup < 0 ? h->alg_bytes[r.cls][r.phase] : h->dgroups[r.dgroup].bytes;
             cnt[r.cls] += 1;
         }
         cudaEventDestroy(r.a);

@@ -62,7 +62,8 @@ struct Task {
     int k0, k1, M, in_ch;
     int out_ch, mix_mode, zero_outs, zero_off;
     int rin_mask, lv_index, p_lo, active;   // p_lo: first part summed by a spread task
-    float scale, pad1;
+    float scale;
+    int dfer;           // 1: the level's fire runs off the step chain (deferred), see engine.cu
     long long origin;   // step at which this PC's time starts (0 for a static bank)
     float2* H;
     float2* X;

@@ -98,9 +98,10 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
     if (tk.T == 1) {   // level 0: parts p >= 2 of block c + 1
         bt = c + 1;
         dst = tk.Yp + (size_t)(bt & 1) * tk.cs;
-    } else {           // parts p >= 1 of the block after the newest fired one
+    } else {           // the block after the newest fired one: parts p >= 1, or
+                       // p >= 2 (double-buffered) for a deferred level
         bt = (c + 1 + tk.s_blocks) / tk.T;
-        dst = tk.Yp;
+        dst = tk.Yp + (tk.dfer ? (size_t)(bt & 1) * tk.cs : 0);
     }
     const int P = tk.P;
     const size_t rs4 = (size_t)(tk.cs >> 1);   // row stride in float4
@@ -152,6 +153,11 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const int N = tk.N, logN = tk.logN, P = tk.P, cs = tk.cs;
     const int N0 = bank.N0;
     const bool l0 = (tk.T == 1);
+    // a deferred fire runs after the step that completed its block (its whole
+    // window is in the input ring) and sums X_b H_0 + X_{b-1} H_1 + Yp[b & 1]
+    // like level 0, with parts >= 2 spread over the level's phases
+    const bool dfer = tk.dfer != 0;
+    const bool two = l0 || dfer;
     float2* s = smem;                 // N complex
     float2* twt = s + N;              // N/2 quarter-wave twiddles
     float2* yacc = twt + N / 2;       // N + 2 (PREFETCH)
@@ -170,13 +176,13 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const long long isamp = rs.io.in_sample;
     const float scale = tk.scale;
     const float2* X1 = tk.X + (size_t)imod(b - 1, P) * cs;   // block b-1 (level 0, p = 1)
-    const float2* Ypb = tk.Yp + (l0 ? (size_t)(b & 1) * cs : 0);
+    const float2* Ypb = tk.Yp + (two ? (size_t)(b & 1) * cs : 0);
 
     const int nq = N >> 1;                       // window quads: samples t_end - 2N + 4q .. + 3
-    const int nq_old = nq - (N0 >> 2);           // quads before this step's input
+    const int nq_old = dfer ? nq : nq - (N0 >> 2);   // quads before this step's input
     const int npair = (N + 2) >> 1;              // bin pairs (float4 of two bins)
-    const bool use_x1 = l0 && P >= 2;
-    const bool use_yp = (l0 && P >= 3) || (!l0 && P >= 2);
+    const bool use_x1 = two && P >= 2;
+    const bool use_yp = (two && P >= 3) || (!two && P >= 2);
 
     // ---- static prologue: nothing earlier steps write (twiddles, filter rows,
     //      this step's input), so it overlaps the previous step's tail -----------
@@ -342,7 +348,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         for (int k = tid; k <= half; k += NT) finish_pair(k, h0s[k], h0s[N - k], yacc[k], yacc[N - k]);
     } else {
         constexpr int CH = C::SPLIT_CH;
-        const bool usey = (l0 && P >= 3) || (!l0 && P >= 2);
+        const bool usey = use_yp;
         for (int k0 = tid; k0 <= half; k0 += CH * NT) {
             float2 h0v[CH][2], av[CH][2];
 #pragma unroll
@@ -358,7 +364,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                         av[u][0] = __ldcg(&Ypb[k]);
                         av[u][1] = __ldcg(&Ypb[bnk]);
                     }
-                    if (l0 && P >= 2) {
+                    if (use_x1) {
                         av[u][0] = cadd(av[u][0], cmul(__ldcg(&X1[k]), __ldg(&tk.H[cs + k])));
                         av[u][1] = cadd(av[u][1], cmul(__ldcg(&X1[bnk]), __ldg(&tk.H[cs + bnk])));
                     }
@@ -609,22 +615,35 @@ cudaError_t prepare_kernels() {
 }
 
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
-                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl) {
+                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio) {
     if (grid <= 0) return cudaSuccess;
+    static int least = 0, greatest = 0;
+    static const bool have_range = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess;
     // programmatic dependent launch: this step's CTAs may be scheduled while
     // the previous step kernel in the stream finishes (their static prologue
     // reads only data no step writes; see cudaGridDependencySynchronize).
     // Callers pass pdl = false when the preceding work is anything else.
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    // A priority lets the block scheduler place the step chain's CTAs ahead
+    // of deferred fires that run beside it.
+    cudaLaunchAttribute attr[2];
+    int na = 0;
+    if (pdl) {
+        attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    if (prio != 0 && have_range) {
+        attr[na].id = cudaLaunchAttributePriority;
+        attr[na].val.priority = prio > 0 ? greatest : least;
+        ++na;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kNT[cls]);
     cfg.dynamicSmemBytes = class_smem_bytes(cls, maxN);
     cfg.stream = st;
     cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
+    cfg.numAttrs = na;
     switch (cls) {
         case 0: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
         case 1: return cudaLaunchKernelEx(&cfg, step_kernel<Cls1>, bank, tasks, rs, rs_dev, step_in_batch);

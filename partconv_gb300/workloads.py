@@ -26,13 +26,17 @@ def decaying_ir(rng: np.random.Generator, length: int, t60: float, fs: int = FS)
     return h.astype(np.float32)
 
 
-def chain_layout(ir_len: int, N0: int, ratio: int = 8, max_block: int = 16384, first_parts: int | None = None):
-    """Minimum-slack ("Gardner") layout: block sizes grow by ``ratio`` per level
-    and every level but the last holds just enough parts for the next level's
-    slack, s_{L+1} = N_{L+1} (the relaxed condition of
-    matlab/MFDL_part_conv.m:25-31).  The last level (<= max_block) takes the
-    rest.  Returns (N, P) with P[-1] recomputed from ir_len."""
-    P0 = first_parts if first_parts is not None else ratio
+def chain_layout(ir_len: int, N0: int, ratio: int = 8, max_block: int = 16384, first_parts: int | None = None,
+                 strict: bool = False):
+    """Level chain: block sizes grow by ``ratio`` per level and every level
+    but the last holds just enough parts for the next level's offset.  Default
+    ("minimum slack", Gardner): s_{L+1} = N_{L+1}, the relaxed condition of
+    matlab/MFDL_part_conv.m:25-31.  strict=True: s_{L+1} = 2 N_{L+1} - 2 N0,
+    the reference's setup condition (src/partconv.cpp:148-170), which leaves
+    each larger level N_{L+1}/N0 - 2 base steps between the completion of a
+    block and its first output sample.  The last level (<= max_block) takes
+    the rest.  Returns (N, P) with P[-1] recomputed from ir_len."""
+    P0 = first_parts if first_parts is not None else (2 * ratio - 2 if strict else ratio)
     N = [N0]
     P = [P0]
     covered = N0 * P0
@@ -40,15 +44,16 @@ def chain_layout(ir_len: int, N0: int, ratio: int = 8, max_block: int = 16384, f
         nb = N[-1] * ratio
         if nb > max_block:
             break
-        # parts of the current level so that s_{L+1} == nb
-        need = nb - (covered - N[-1] * P[-1])
+        # parts of the current level so that s_{L+1} reaches its target
+        target = 2 * nb - 2 * N0 if strict else nb
+        need = target - (covered - N[-1] * P[-1])
         P[-1] = max(P[-1], -(-need // N[-1]))
         covered = sum(n * p for n, p in zip(N, P))
         if covered >= ir_len:
             break
         N.append(nb)
-        P.append(ratio - 1)
-        covered += nb * (ratio - 1)
+        P.append(2 * ratio - 2 if strict else ratio - 1)
+        covered += nb * P[-1]
     s_last = sum(n * p for n, p in zip(N[:-1], P[:-1]))
     P[-1] = max(1, -(-(ir_len - s_last) // N[-1]))
     return N, P

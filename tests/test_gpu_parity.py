@@ -36,7 +36,13 @@ LAYOUTS = [
     ([512, 4096], [8, 15], 65536),         # config 4 layout
     ([32, 64, 128, 256], [2, 1, 1, 0], 1500),
     ([1024, 8192], [8, 3], 30000),         # class-2 FFT size
+    # layouts with slack: larger levels' fires are deferred off the step chain
+    ([64, 512, 4096], [14, 14, 0], 40000),        # strict ratio 8: windows 6 and 62 steps
+    ([128, 1024], [40, 0], 12000),                # slack 32 steps, window capped at T - 2 = 6
+    ([64, 512], [9, 0], 6000),                    # window of one step
+    ([256, 2048, 16384], [14, 14, 0], 131072),    # config-1 IR length, strict chain
 ]
+DEFERRED = LAYOUTS[7:]
 
 
 @pytest.mark.parametrize("N,P,L", LAYOUTS)
@@ -57,7 +63,7 @@ def test_single_pc_run_matches_oracle(gpu, N, P, L):
     assert m.kernel_launches() > 0
 
 
-@pytest.mark.parametrize("N,P,L", LAYOUTS[1:4])
+@pytest.mark.parametrize("N,P,L", LAYOUTS[1:4] + DEFERRED)
 def test_process_graph_path_equals_callbacks(gpu, N, P, L):
     """pc_process (graph replays) gives bit-identical results to pc_run."""
     rng = np.random.default_rng(L + 1)
@@ -184,3 +190,27 @@ def test_config2_batched_full_size(gpu):
     ref, _ = oracle.run_streams(c["layouts"], c["irs"], x, N0)
     for s in range(S):
         assert wl.rel_l2(y[s], ref[s]) <= TOL, s
+
+
+def test_deferred_and_in_step_levels_mixed(gpu):
+    """One handle with PCs whose larger levels fire within their step (slack
+    0) and PCs whose larger levels are deferred, summed into shared outputs."""
+    rng = np.random.default_rng(77)
+    N0 = 128
+    specs = [dict(N=[128, 1024], P=[8, 0], L=9000, in_ch=0, out_ch=0),
+             dict(N=[128, 1024, 8192], P=[14, 14, 0], L=40000, in_ch=1, out_ch=0),
+             dict(N=[128, 512, 2048], P=[6, 6, 0], L=7000, in_ch=0, out_ch=1),
+             dict(N=[128, 1024], P=[20, 0], L=12000, in_ch=1, out_ch=1, scale=0.5)]
+    pcs = [dict(ir=_ir(rng, s_["L"]), N=s_["N"], P=s_["P"], in_ch=s_["in_ch"], out_ch=s_["out_ch"],
+                scale=s_.get("scale", 1.0)) for s_ in specs]
+    frames = N0 * 700
+    x = (0.1 * rng.standard_normal((frames, 2))).astype(np.float32)
+    m = PartConvMulti()
+    m.setup_layout(48000, N0, 2, 2, pcs)
+    y = m.process(x)
+    ref = oracle.OracleMulti(N0, 2, 2, pcs).run(x)
+    for o in range(2):
+        assert wl.rel_l2(y[:, o], ref[:, o]) <= TOL
+    m.reset()
+    yc = _run_callbacks(m, x, N0)
+    assert np.array_equal(y, yc)

@@ -186,6 +186,32 @@ typedef struct pc_kernel_stats {
  */
 int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int max_kinds, int* n_kinds);
 
+/* Statistics of one pc_rt_drive run (times in microseconds). */
+typedef struct pc_rt_stats {
+    long long callbacks;      /* blocks processed */
+    long long misses;         /* callbacks that returned after their deadline */
+    double period_us;         /* block period */
+    double compute_mean_us;   /* mean time inside pc_run */
+    double latency_p50_us;    /* release-to-return time (compute time when not real-time) */
+    double latency_p99_us;
+    double latency_max_us;
+    double wall_s;            /* wall time of the run */
+} pc_rt_stats;
+
+/*
+ * Headless real-time driver, in place of the audio callback loop of the
+ * reference's programs (src/pcRTMulti.cpp:138-185 PortAudio, :303-506 ALSA,
+ * which count output underflows).  Calls pc_run once per block of
+ * buffer_size frames, releasing callback k at k periods after the start on a
+ * monotonic clock (realtime != 0; 0 runs back to back), and counts a miss
+ * when a callback returns after the next release, the time the device would
+ * play its block.  period_s <= 0 means buffer_size / fs.  `in` / `out` are
+ * interleaved host buffers of `frames` frames (a multiple of buffer_size).
+ * The handle's frame counter advances as with pc_run.
+ */
+int pc_rt_drive(pc_handle* h, const float* in, float* out, long long frames, double period_s, int realtime,
+                pc_rt_stats* stats);
+
 /* ---------------------------------------------------------------------------
  * PartConvFilter: one partitioned convolver driven level by level, the class
  * the reference's Python module exposes (src/partconv.h:40-114, wrapped by

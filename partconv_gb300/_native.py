@@ -53,6 +53,19 @@ class PCKernelStats(C.Structure):
     ]
 
 
+class PCRtStats(C.Structure):
+    _fields_ = [
+        ("callbacks", C.c_longlong),
+        ("misses", C.c_longlong),
+        ("period_us", C.c_double),
+        ("compute_mean_us", C.c_double),
+        ("latency_p50_us", C.c_double),
+        ("latency_p99_us", C.c_double),
+        ("latency_max_us", C.c_double),
+        ("wall_s", C.c_double),
+    ]
+
+
 # name -> (restype, argtypes); mirrors include/partconv_gb300.h
 SIGNATURES = {
     "pc_check_layout": (C.c_int, [C.c_int, _i32p, _i32p, C.c_int, C.c_int, _i32p, C.c_char_p, C.c_int]),
@@ -73,6 +86,7 @@ SIGNATURES = {
     "pc_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "pc_profile_kernels": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(PCKernelStats), C.c_int,
                                      C.POINTER(C.c_int)]),
+    "pc_rt_drive": (C.c_int, [C.c_void_p, _f32p, _f32p, C.c_longlong, C.c_double, C.c_int, C.POINTER(PCRtStats)]),
     "pc_convolve_noalloc": (C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                       C.c_void_p]),
     "pcf_create": (C.c_void_p, [C.c_int, C.c_int]),

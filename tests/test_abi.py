@@ -90,6 +90,11 @@ def test_calls_before_setup_return_errors():
     y = np.zeros(256, np.float32)
     assert lib.pc_run(h, y.ctypes.data_as(nat._f32p), x.ctypes.data_as(nat._f32p), 256) == nat.PC_ERR_STATE
     assert b"setup" in lib.pc_last_error(h)
+    st = nat.PCRtStats()
+    assert lib.pc_rt_drive(h, x.ctypes.data_as(nat._f32p), y.ctypes.data_as(nat._f32p), 256, 0.0, 0,
+                           C.byref(st)) != nat.PC_OK
+    assert lib.pc_rt_drive(None, x.ctypes.data_as(nat._f32p), y.ctypes.data_as(nat._f32p), 256, 0.0, 0,
+                           C.byref(st)) == nat.PC_ERR_ARG
     assert lib.pc_reset(h) == nat.PC_OK
     assert lib.pc_cleanup(h) == nat.PC_OK
     lib.pc_destroy(h)

@@ -214,3 +214,28 @@ def test_deferred_and_in_step_levels_mixed(gpu):
     m.reset()
     yc = _run_callbacks(m, x, N0)
     assert np.array_equal(y, yc)
+
+
+def test_rt_driver_matches_callbacks_and_reports(gpu):
+    """Headless real-time driver: same samples as pc_run callbacks, one
+    callback per 256-sample period at 48 kHz, latency and misses reported."""
+    from partconv_gb300.rtdriver import RealtimeDriver
+
+    rng = np.random.default_rng(5)
+    N, P, L = [256, 2048, 16384], [14, 14, 0], 60000
+    h = _ir(rng, L)
+    frames = 256 * 120
+    x = (0.1 * rng.standard_normal((frames, 1))).astype(np.float32)
+    m = PartConvMulti()
+    m.setup_layout(48000, 256, 1, 1, [dict(ir=h, N=N, P=P)])
+    y_cb = _run_callbacks(m, x, 256)
+    m.reset()
+    y, st = RealtimeDriver(m).run(x, realtime=True)
+    assert np.array_equal(y, y_cb)
+    assert st["callbacks"] == 120 and abs(st["period_us"] - 1e6 * 256 / 48000) < 1e-6
+    assert 0 < st["latency_p50_us"] <= st["latency_p99_us"] <= st["latency_max_us"]
+    assert st["wall_s"] >= 120 * 256 / 48000 * 0.99
+    print("rt driver:", {k: round(v, 2) for k, v in st.items()})
+    m.reset()
+    y2, st2 = RealtimeDriver(m).run(x, realtime=False)
+    assert np.array_equal(y2, y_cb) and st2["misses"] == 0

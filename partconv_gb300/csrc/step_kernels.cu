@@ -145,7 +145,15 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
 }
 
 // ---------------------------------------------------------------------------
-template <class C>
+// EARLY (step kernels): a level-0 fire whose whole window lies in this
+// call's input does its forward transform, writes its spectrum and forms
+// X_b H_0 before waiting for the previous step; only X_{b-1} H_1 + Yp, the
+// inverse transform and the output follow the wait.  That is safe because a
+// step kernel signals its dependents only after its own wait: when this
+// kernel starts, the step before the previous one has completed, and the
+// previous one no longer reads this step's spectrum slot (its spread tasks
+// read slots b-2 .. b-P+1).
+template <class C, bool EARLY>
 __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, const RunState& rs, long long c,
                                           float2* smem, int* s_last) {
     constexpr int NT = C::NT;
@@ -183,9 +191,41 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const int npair = (N + 2) >> 1;              // bin pairs (float4 of two bins)
     const bool use_x1 = two && P >= 2;
     const bool use_yp = (two && P >= 3) || (!two && P >= 2);
+    const bool early = EARLY && C::PREFETCH && l0 && io_step >= 1;
+    const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
+    // the other levels' due output slices, summed in level order into `emit`
+    // (their fires completed before this launch: full graph/stream edges)
+    auto gather_emit = [&]() {
+        if constexpr (C::PREFETCH) {
+            float4 ev[C::PREFETCH ? C::MAXE : 1][kEmitLevels];
+#pragma unroll
+            for (int i = 0; i < C::MAXE; ++i) {
+                const int e4 = tid + i * NT;
+#pragma unroll
+                for (int L = 0; L < kEmitLevels; ++L)
+                    if (L < Le && 4 * e4 < N0)
+                        ev[i][L] = __ldcg(reinterpret_cast<const float4*>(tk.eyring[L] + ((t_new + 4 * e4) & tk.emask[L])));
+            }
+#pragma unroll
+            for (int i = 0; i < C::MAXE; ++i) {
+                const int e4 = tid + i * NT;
+                if (4 * e4 >= N0) continue;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int L = 0; L < kEmitLevels; ++L)
+                    if (L < Le) v = f4add(v, ev[i][L]);
+                for (int L = kEmitLevels + 1; L < tk.M; ++L) {   // rare: more than 5 levels
+                    const DevLevel& l2 = bank.lv[tk.lv_index + L];
+                    v = f4add(v, __ldcg(reinterpret_cast<const float4*>(l2.yring + ((t_new + 4 * e4) & l2.rmask))));
+                }
+                *reinterpret_cast<float4*>(emit + 4 * e4) = v;
+            }
+        }
+    };
 
-    // ---- static prologue: nothing earlier steps write (twiddles, filter rows,
-    //      this step's input), so it overlaps the previous step's tail -----------
+    // ---- static prologue: data no running kernel writes (twiddles, filter
+    //      rows, this call's input; in the EARLY case also the other levels'
+    //      due output slices), so it overlaps the previous step's tail ----------
     {
         float4 wv[C::MAXQ];
 #pragma unroll
@@ -195,6 +235,11 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                 const long long j = 4LL * (qd - nq_old);
                 wv[i] = make_float4(in[j * isamp] * scale, in[(j + 1) * isamp] * scale, in[(j + 2) * isamp] * scale,
                                     in[(j + 3) * isamp] * scale);
+            } else if (early && qd < nq_old) {   // previous block, from the call's input
+                const float* pin = in - rs.io.in_step;
+                const long long j = 4LL * qd;
+                wv[i] = make_float4(pin[j * isamp] * scale, pin[(j + 1) * isamp] * scale,
+                                    pin[(j + 2) * isamp] * scale, pin[(j + 3) * isamp] * scale);
             }
         }
         const int ntw = N >> 1;
@@ -219,11 +264,16 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
 #pragma unroll
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
-            if (qd >= nq_old && qd < nq) {
+            if ((qd >= nq_old || early) && qd < nq) {
                 s[2 * qd] = make_float2(wv[i].x, wv[i].y);
                 s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
+                if (early && qd >= nq_old) {   // append this step's input to the PC's ring
+                    const long long ta = t_end - 2LL * N + 4LL * qd;
+                    *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
+                }
             }
         }
+        if (early) gather_emit();
 #pragma unroll
         for (int i = 0; i < C::MAXT; ++i) {
             const int m = tid + i * NT;
@@ -241,8 +291,58 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         }
     }
 
-    // earlier steps' kernels have completed and their writes are visible
+    float2* __restrict__ Xs = tk.X + (size_t)slot * cs;
+    const int half = N >> 1;
+    if (early) {
+        // forward transform, spectrum X_b, and X_b H_0 (kept in h0s; bin
+        // N - half of the self-paired k = half goes to the pad slot N + 1)
+        __syncthreads();
+        fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
+        for (int k = tid; k <= half; k += NT) {
+            const int nk = (k == 0) ? 0 : N - k;
+            float2 xk, xnk;
+            rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
+            const int bnk = N - k;
+            Xs[k] = xk;
+            if (bnk != k) Xs[bnk] = xnk;
+            const float2 pk = cmul(xk, h0s[k]);
+            const float2 pnk = cmul(xnk, h0s[bnk]);
+            h0s[k] = pk;
+            h0s[bnk != k ? bnk : N + 1] = pnk;
+        }
+    }
+
+    // earlier steps' kernels have completed and their writes are visible; the
+    // next step's kernel may now start its own independent part
     cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
+
+    if (early) {
+        // X_{b-1} H_1 + Yp[b & 1], then the inverse merge
+#pragma unroll
+        for (int i = 0; i < C::MAXK; ++i) {
+            const int kk = 2 * (tid + i * NT);
+            if (kk < 2 * npair) {
+                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (use_x1)
+                    acc = f4mul(__ldcg(reinterpret_cast<const float4*>(X1 + kk)),
+                                *reinterpret_cast<const float4*>(yacc + kk));
+                if (use_yp) acc = f4add(acc, __ldcg(reinterpret_cast<const float4*>(Ypb + kk)));
+                *reinterpret_cast<float4*>(yacc + kk) = acc;
+            }
+        }
+        __syncthreads();
+        for (int k = tid; k <= half; k += NT) {
+            const int bnk = N - k;
+            const float2 yk = cadd(h0s[k], yacc[k]);
+            const float2 ynk = cadd(h0s[bnk != k ? bnk : N + 1], yacc[bnk]);
+            float2 zk, znk;
+            irfft_merge(yk, ynk, k, logN, tw, zk, znk);
+            s[k] = zk;
+            if (k != 0 && k != half) s[N - k] = znk;
+        }
+        __syncthreads();
+    } else {
 
     // ---- dynamic prologue: input ring, previous spectrum, partial sums and the
     //      other levels' output rings (written by earlier steps) ---------------------
@@ -257,8 +357,6 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             }
         }
         float4 xa[C::PREFETCH ? C::MAXK : 1], ya[C::PREFETCH ? C::MAXK : 1];
-        float4 ev[C::PREFETCH ? C::MAXE : 1][kEmitLevels];
-        const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
         if (C::PREFETCH) {
 #pragma unroll
             for (int i = 0; i < C::MAXK; ++i) {
@@ -266,17 +364,6 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                 if (kk < 2 * npair) {
                     if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
                     if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
-                }
-            }
-            if (l0) {
-#pragma unroll
-                for (int i = 0; i < C::MAXE; ++i) {
-                    const int e4 = tid + i * NT;
-#pragma unroll
-                    for (int L = 0; L < kEmitLevels; ++L)
-                        if (L < Le && 4 * e4 < N0)
-                            ev[i][L] = __ldcg(reinterpret_cast<const float4*>(
-                                tk.eyring[L] + ((t_new + 4 * e4) & tk.emask[L])));
                 }
             }
         }
@@ -305,22 +392,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                     *reinterpret_cast<float4*>(yacc + kk) = acc;
                 }
             }
-            if (l0) {
-#pragma unroll
-                for (int i = 0; i < C::MAXE; ++i) {
-                    const int e4 = tid + i * NT;
-                    if (4 * e4 >= N0) continue;
-                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                    for (int L = 0; L < kEmitLevels; ++L)
-                        if (L < Le) v = f4add(v, ev[i][L]);
-                    for (int L = kEmitLevels + 1; L < tk.M; ++L) {   // rare: more than 5 levels
-                        const DevLevel& l2 = bank.lv[tk.lv_index + L];
-                        v = f4add(v, __ldcg(reinterpret_cast<const float4*>(l2.yring + ((t_new + 4 * e4) & l2.rmask))));
-                    }
-                    *reinterpret_cast<float4*>(emit + 4 * e4) = v;
-                }
-            }
+            if (l0) gather_emit();
         }
     }
     __syncthreads();
@@ -328,8 +400,6 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
 
     // ---- split, FDL MAC, inverse merge -------------------------------------------
-    float2* __restrict__ Xs = tk.X + (size_t)slot * cs;
-    const int half = N >> 1;
     auto finish_pair = [&](int k, float2 h0k, float2 h0nk, float2 ak, float2 ank) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
@@ -378,6 +448,8 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         }
     }
     __syncthreads();
+
+    }
 
     fft_smem<NT, C::MAXB>(s, N, logN, tw, true);
 
@@ -444,9 +516,9 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     __shared__ __align__(16) RunState rs;
     __shared__ int s_last;
     const int tid = threadIdx.x;
-    // the next step's CTAs may start their static prologue now; they wait in
-    // cudaGridDependencySynchronize() until this grid has completed
-    cudaTriggerProgrammaticLaunchCompletion();
+    // The next step's kernel is signalled only after this grid's dependency
+    // wait (in fire_body and below), so its independent part never overlaps
+    // a kernel older than this one.
     if (tid < 12) {
         reinterpret_cast<int4*>(&tk)[tid] = __ldg(reinterpret_cast<const int4*>(tasks + blockIdx.x) + tid);
     } else if (tid >= 32 && tid < 37) {
@@ -458,10 +530,11 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     const long long c = rs.step_base + step_in_batch;
     if (tk.kind == 1) {
         cudaGridDependencySynchronize();
+        cudaTriggerProgrammaticLaunchCompletion();
         spread_body<C::NT>(tk, c, dyn_smem);
         return;
     }
-    fire_body<C>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
+    fire_body<C, true>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
 }
 
 // ---------------------------------------------------------------------------
@@ -491,7 +564,7 @@ __global__ void __launch_bounds__(C::NT) pool_kernel(Bank bank, const Task* __re
     const long long q = cl + 1 + tk.s_blocks;
     if (pm.sub == 0) {
         if (q % tk.T != 0) return;
-        fire_body<C>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
+        fire_body<C, false>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
         return;
     }
     int lo, hi, p_lo;

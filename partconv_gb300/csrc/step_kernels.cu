@@ -224,10 +224,12 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     };
 
     // ---- static prologue: data no running kernel writes (twiddles, filter
-    //      rows, this call's input; in the EARLY case also the other levels'
-    //      due output slices), so it overlaps the previous step's tail ----------
+    //      rows, this call's input), so it overlaps the previous step's tail.
+    //      The input-ring append and the other levels' output slices wait for
+    //      the dependency (a larger level of the same kernel class may still
+    //      be reading the ring and writing its output in the previous step).
+    float4 wv[C::MAXQ];
     {
-        float4 wv[C::MAXQ];
 #pragma unroll
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
@@ -267,13 +269,8 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             if ((qd >= nq_old || early) && qd < nq) {
                 s[2 * qd] = make_float2(wv[i].x, wv[i].y);
                 s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
-                if (early && qd >= nq_old) {   // append this step's input to the PC's ring
-                    const long long ta = t_end - 2LL * N + 4LL * qd;
-                    *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
-                }
             }
         }
-        if (early) gather_emit();
 #pragma unroll
         for (int i = 0; i < C::MAXT; ++i) {
             const int m = tid + i * NT;
@@ -318,16 +315,33 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     cudaTriggerProgrammaticLaunchCompletion();
 
     if (early) {
-        // X_{b-1} H_1 + Yp[b & 1], then the inverse merge
+        // X_{b-1} H_1 + Yp[b & 1], the other levels' due slices and the
+        // input-ring append, then the inverse merge
+        float4 xa[C::MAXK], ya[C::MAXK];
+#pragma unroll
+        for (int i = 0; i < C::MAXK; ++i) {
+            const int kk = 2 * (tid + i * NT);
+            if (kk < 2 * npair) {
+                if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
+                if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
+            }
+        }
+        gather_emit();
+#pragma unroll
+        for (int i = 0; i < C::MAXQ; ++i) {
+            const int qd = tid + i * NT;
+            if (qd >= nq_old && qd < nq) {
+                const long long ta = t_end - 2LL * N + 4LL * qd;
+                *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
+            }
+        }
 #pragma unroll
         for (int i = 0; i < C::MAXK; ++i) {
             const int kk = 2 * (tid + i * NT);
             if (kk < 2 * npair) {
                 float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (use_x1)
-                    acc = f4mul(__ldcg(reinterpret_cast<const float4*>(X1 + kk)),
-                                *reinterpret_cast<const float4*>(yacc + kk));
-                if (use_yp) acc = f4add(acc, __ldcg(reinterpret_cast<const float4*>(Ypb + kk)));
+                if (use_x1) acc = f4mul(xa[i], *reinterpret_cast<const float4*>(yacc + kk));
+                if (use_yp) acc = f4add(acc, ya[i]);
                 *reinterpret_cast<float4*>(yacc + kk) = acc;
             }
         }
@@ -347,13 +361,13 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     // ---- dynamic prologue: input ring, previous spectrum, partial sums and the
     //      other levels' output rings (written by earlier steps) ---------------------
     {
-        float4 wv[C::MAXQ];
+        float4 wo[C::MAXQ];
 #pragma unroll
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
             if (qd < nq_old) {
                 const long long ta = t_end - 2LL * N + 4LL * qd;
-                wv[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
+                wo[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
             }
         }
         float4 xa[C::PREFETCH ? C::MAXK : 1], ya[C::PREFETCH ? C::MAXK : 1];
@@ -371,8 +385,8 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
             if (qd < nq_old) {
-                s[2 * qd] = make_float2(wv[i].x, wv[i].y);
-                s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
+                s[2 * qd] = make_float2(wo[i].x, wo[i].y);
+                s[2 * qd + 1] = make_float2(wo[i].z, wo[i].w);
             } else if (l0 && qd < nq) {
                 // level 0 appends this step's input to the PC's ring (read back
                 // from the thread's own shared-memory writes)

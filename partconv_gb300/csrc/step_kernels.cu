@@ -290,9 +290,12 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
 
     float2* __restrict__ Xs = tk.X + (size_t)slot * cs;
     const int half = N >> 1;
-    if (early) {
-        // forward transform, spectrum X_b, and X_b H_0 (kept in h0s; bin
-        // N - half of the self-paired k = half goes to the pad slot N + 1)
+
+    // Prefetch classes run the split/MAC/merge in two passes with X_b H_0
+    // parked in shared memory, whether or not the forward transform ran
+    // before the dependency wait: one sequence of float operations, so the
+    // EARLY and the in-order paths give identical bits.
+    auto forward_pass = [&]() {   // forward FFT, X_b, X_b H_0 -> h0s (k = half: N - k product in slot N + 1)
         __syncthreads();
         fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
         for (int k = tid; k <= half; k += NT) {
@@ -307,44 +310,8 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             h0s[k] = pk;
             h0s[bnk != k ? bnk : N + 1] = pnk;
         }
-    }
-
-    // earlier steps' kernels have completed and their writes are visible; the
-    // next step's kernel may now start its own independent part
-    cudaGridDependencySynchronize();
-    cudaTriggerProgrammaticLaunchCompletion();
-
-    if (early) {
-        // X_{b-1} H_1 + Yp[b & 1], the other levels' due slices and the
-        // input-ring append, then the inverse merge
-        float4 xa[C::MAXK], ya[C::MAXK];
-#pragma unroll
-        for (int i = 0; i < C::MAXK; ++i) {
-            const int kk = 2 * (tid + i * NT);
-            if (kk < 2 * npair) {
-                if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
-                if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
-            }
-        }
-        gather_emit();
-#pragma unroll
-        for (int i = 0; i < C::MAXQ; ++i) {
-            const int qd = tid + i * NT;
-            if (qd >= nq_old && qd < nq) {
-                const long long ta = t_end - 2LL * N + 4LL * qd;
-                *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < C::MAXK; ++i) {
-            const int kk = 2 * (tid + i * NT);
-            if (kk < 2 * npair) {
-                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (use_x1) acc = f4mul(xa[i], *reinterpret_cast<const float4*>(yacc + kk));
-                if (use_yp) acc = f4add(acc, ya[i]);
-                *reinterpret_cast<float4*>(yacc + kk) = acc;
-            }
-        }
+    };
+    auto merge_pass = [&]() {     // Y = X_b H_0 + (X_{b-1} H_1 + Yp), inverse merge into s
         __syncthreads();
         for (int k = tid; k <= half; k += NT) {
             const int bnk = N - k;
@@ -356,83 +323,111 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             if (k != 0 && k != half) s[N - k] = znk;
         }
         __syncthreads();
-    } else {
-
-    // ---- dynamic prologue: input ring, previous spectrum, partial sums and the
-    //      other levels' output rings (written by earlier steps) ---------------------
-    {
-        float4 wo[C::MAXQ];
-#pragma unroll
-        for (int i = 0; i < C::MAXQ; ++i) {
-            const int qd = tid + i * NT;
-            if (qd < nq_old) {
-                const long long ta = t_end - 2LL * N + 4LL * qd;
-                wo[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
-            }
-        }
-        float4 xa[C::PREFETCH ? C::MAXK : 1], ya[C::PREFETCH ? C::MAXK : 1];
-        if (C::PREFETCH) {
-#pragma unroll
-            for (int i = 0; i < C::MAXK; ++i) {
-                const int kk = 2 * (tid + i * NT);
-                if (kk < 2 * npair) {
-                    if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
-                    if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
-                }
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < C::MAXQ; ++i) {
-            const int qd = tid + i * NT;
-            if (qd < nq_old) {
-                s[2 * qd] = make_float2(wo[i].x, wo[i].y);
-                s[2 * qd + 1] = make_float2(wo[i].z, wo[i].w);
-            } else if (l0 && qd < nq) {
-                // level 0 appends this step's input to the PC's ring (read back
-                // from the thread's own shared-memory writes)
-                const long long ta = t_end - 2LL * N + 4LL * qd;
-                const float2 a = s[2 * qd], bb = s[2 * qd + 1];
-                *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = make_float4(a.x, a.y, bb.x, bb.y);
-            }
-        }
-        if (C::PREFETCH) {
-#pragma unroll
-            for (int i = 0; i < C::MAXK; ++i) {
-                const int kk = 2 * (tid + i * NT);
-                if (kk < 2 * npair) {
-                    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (use_x1) acc = f4mul(xa[i], *reinterpret_cast<const float4*>(yacc + kk));
-                    if (use_yp) acc = f4add(acc, ya[i]);
-                    *reinterpret_cast<float4*>(yacc + kk) = acc;
-                }
-            }
-            if (l0) gather_emit();
-        }
-    }
-    __syncthreads();
-
-    fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
-
-    // ---- split, FDL MAC, inverse merge -------------------------------------------
-    auto finish_pair = [&](int k, float2 h0k, float2 h0nk, float2 ak, float2 ank) {
-        const int nk = (k == 0) ? 0 : N - k;
-        float2 xk, xnk;
-        rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
-        const int bk = k, bnk = N - k;   // k == 0 pairs bin 0 with bin N
-        Xs[bk] = xk;
-        if (bnk != bk) Xs[bnk] = xnk;
-        const float2 yk = cadd(cmul(xk, h0k), ak);
-        const float2 ynk = cadd(cmul(xnk, h0nk), ank);
-        float2 zk, znk;
-        irfft_merge(yk, ynk, k, logN, tw, zk, znk);
-        s[k] = zk;
-        if (k != 0 && k != half) s[N - k] = znk;
     };
-    if (C::PREFETCH) {
-        for (int k = tid; k <= half; k += NT) finish_pair(k, h0s[k], h0s[N - k], yacc[k], yacc[N - k]);
+    // yacc (holding H_1) <- X_{b-1} H_1 + Yp[b & 1], same float4 mapping as the prefetch
+    auto partial_pass = [&](const float4* xa, const float4* ya) {
+#pragma unroll
+        for (int i = 0; i < C::MAXK; ++i) {
+            const int kk = 2 * (tid + i * NT);
+            if (kk < 2 * npair) {
+                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (use_x1) acc = f4mul(xa[i], *reinterpret_cast<const float4*>(yacc + kk));
+                if (use_yp) acc = f4add(acc, ya[i]);
+                *reinterpret_cast<float4*>(yacc + kk) = acc;
+            }
+        }
+    };
+
+    if (early) forward_pass();
+
+    // earlier steps' kernels have completed and their writes are visible; the
+    // next step's kernel may now start its own independent part
+    cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
+
+    if constexpr (C::PREFETCH) {
+        // ---- dependent inputs: input-ring history (unless EARLY), previous
+        //      spectrum, partial sums, the other levels' due output slices ----
+        float4 wo[C::MAXQ], xa[C::MAXK], ya[C::MAXK];
+        if (!early) {
+#pragma unroll
+            for (int i = 0; i < C::MAXQ; ++i) {
+                const int qd = tid + i * NT;
+                if (qd < nq_old) {
+                    const long long ta = t_end - 2LL * N + 4LL * qd;
+                    wo[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < C::MAXK; ++i) {
+            const int kk = 2 * (tid + i * NT);
+            if (kk < 2 * npair) {
+                if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
+                if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
+            }
+        }
+        if (l0) gather_emit();
+#pragma unroll
+        for (int i = 0; i < C::MAXQ; ++i) {
+            const int qd = tid + i * NT;
+            if (qd < nq_old) {
+                if (!early) {
+                    s[2 * qd] = make_float2(wo[i].x, wo[i].y);
+                    s[2 * qd + 1] = make_float2(wo[i].z, wo[i].w);
+                }
+            } else if (l0 && qd < nq) {   // level 0 appends this step's input to the PC's ring
+                const long long ta = t_end - 2LL * N + 4LL * qd;
+                *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
+            }
+        }
+        partial_pass(xa, ya);
+        if (!early) forward_pass();
+        merge_pass();
     } else {
+        // ---- dependent inputs (no prefetch): input-ring history ----------------
+        {
+            float4 wo[C::MAXQ];
+#pragma unroll
+            for (int i = 0; i < C::MAXQ; ++i) {
+                const int qd = tid + i * NT;
+                if (qd < nq_old) {
+                    const long long ta = t_end - 2LL * N + 4LL * qd;
+                    wo[i] = __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask)));
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < C::MAXQ; ++i) {
+                const int qd = tid + i * NT;
+                if (qd < nq_old) {
+                    s[2 * qd] = make_float2(wo[i].x, wo[i].y);
+                    s[2 * qd + 1] = make_float2(wo[i].z, wo[i].w);
+                } else if (l0 && qd < nq) {   // append, read back from this thread's own writes
+                    const long long ta = t_end - 2LL * N + 4LL * qd;
+                    const float2 a = s[2 * qd], bb = s[2 * qd + 1];
+                    *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = make_float4(a.x, a.y, bb.x, bb.y);
+                }
+            }
+        }
+        __syncthreads();
+        fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
+
+        // ---- split, FDL MAC, inverse merge, operands streamed from L2 ----------
+        auto finish_pair = [&](int k, float2 h0k, float2 h0nk, float2 ak, float2 ank) {
+            const int nk = (k == 0) ? 0 : N - k;
+            float2 xk, xnk;
+            rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
+            const int bk = k, bnk = N - k;   // k == 0 pairs bin 0 with bin N
+            Xs[bk] = xk;
+            if (bnk != bk) Xs[bnk] = xnk;
+            const float2 yk = cadd(cmul(xk, h0k), ak);
+            const float2 ynk = cadd(cmul(xnk, h0nk), ank);
+            float2 zk, znk;
+            irfft_merge(yk, ynk, k, logN, tw, zk, znk);
+            s[k] = zk;
+            if (k != 0 && k != half) s[N - k] = znk;
+        };
         constexpr int CH = C::SPLIT_CH;
-        const bool usey = use_yp;
         for (int k0 = tid; k0 <= half; k0 += CH * NT) {
             float2 h0v[CH][2], av[CH][2];
 #pragma unroll
@@ -444,7 +439,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                     h0v[u][1] = __ldg(&tk.H[bnk]);
                     av[u][0] = make_float2(0.f, 0.f);
                     av[u][1] = av[u][0];
-                    if (usey) {
+                    if (use_yp) {
                         av[u][0] = __ldcg(&Ypb[k]);
                         av[u][1] = __ldcg(&Ypb[bnk]);
                     }
@@ -460,9 +455,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                 if (k <= half) finish_pair(k, h0v[u][0], h0v[u][1], av[u][0], av[u][1]);
             }
         }
-    }
-    __syncthreads();
-
+        __syncthreads();
     }
 
     fft_smem<NT, C::MAXB>(s, N, logN, tw, true);

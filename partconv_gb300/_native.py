@@ -6,6 +6,7 @@ call needs a GPU that is not there, the error propagates.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
 
 from . import _build
@@ -138,11 +139,12 @@ _lib = None
 
 
 def lib(build: bool = True):
-    """Load the in-tree library (building it first when sources changed)."""
+    """Load the in-tree library (building it first when sources changed), or
+    the library named by $PARTCONV_GB300_LIB (a build with other options)."""
     global _lib
     with _lock:
         if _lib is None:
-            path = _build.build() if build else _build.LIB_PATH
+            path = os.environ.get("PARTCONV_GB300_LIB") or (_build.build() if build else _build.LIB_PATH)
             L = C.CDLL(path)
             for name, (res, args) in SIGNATURES.items():
                 fn = getattr(L, name)

@@ -185,7 +185,6 @@ struct pc_handle {
 
     long long frame_num = 0;
     long long launches = 0;
-    bool direct_prev_l0 = false;   // last direct launch was a level-0 class kernel
 };
 
 namespace {
@@ -233,22 +232,17 @@ int phase_of(const pc_handle* h, long long step) { return (int)(step & (long lon
 
 // One base step by direct launches (classes with work in this phase).
 // first: the preceding work in the stream is not one of this handle's step
-// kernels, so the launch must not overlap it.  A level-0 kernel overlaps
-// only the previous step's level-0 kernel: before its dependency wait it may
-// read the other levels' output rings, which the previous step's other
-// kernels may still be writing.
+// kernels, so the launch must not overlap it.
 int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool first) {
     const int ph = phase_of(h, rs.step_base);
     for (int k = 0; k < kClasses; ++k) {
         const int cls = (h->l0_class + k) % kClasses;   // level-0 class first
         const int n = h->cnt[cls][ph];
         if (n <= 0) continue;
-        const bool pdl = !first && (cls != h->l0_class || h->direct_prev_l0);
         CK(launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs, nullptr, 0, st,
-                             pdl),
+                             !first),
            "step launch");
         first = false;
-        h->direct_prev_l0 = (cls == h->l0_class);
         h->launches += 1;
     }
     // deferred fires of blocks completed by this step, in stream order (a
@@ -259,7 +253,6 @@ int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool f
                              !first),
            "deferred fire launch");
         first = false;
-        h->direct_prev_l0 = false;
         h->launches += 1;
     }
     return PC_OK;

@@ -146,13 +146,13 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
 
 // ---------------------------------------------------------------------------
 // EARLY (step kernels): a level-0 fire whose whole window lies in this
-// call's input does its forward transform, writes its spectrum and forms
-// X_b H_0 before waiting for the previous step; only X_{b-1} H_1 + Yp, the
-// inverse transform and the output follow the wait.  That is safe because a
-// step kernel signals its dependents only after its own wait: when this
-// kernel starts, the step before the previous one has completed, and the
-// previous one no longer reads this step's spectrum slot (its spread tasks
-// read slots b-2 .. b-P+1).
+// call's input runs its forward transform and forms X_b H_0 before waiting
+// for the previous step, keeping X_b in registers; only the global writes
+// (X_b, the input-ring append), X_{b-1} H_1 + Yp, the inverse transform and
+// the output follow the wait.  Before the wait a step kernel reads only data
+// no kernel writes (input, twiddles, filter spectra) and writes only shared
+// memory, so it may overlap any number of earlier step kernels: it signals
+// its dependents at entry.
 template <class C, bool EARLY>
 __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, const RunState& rs, long long c,
                                           float2* smem, int* s_last) {
@@ -295,16 +295,22 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     // parked in shared memory, whether or not the forward transform ran
     // before the dependency wait: one sequence of float operations, so the
     // EARLY and the in-order paths give identical bits.
+    float2 xr[C::MAXK][2];   // EARLY: this thread's X_b pairs until after the wait
     auto forward_pass = [&]() {   // forward FFT, X_b, X_b H_0 -> h0s (k = half: N - k product in slot N + 1)
         __syncthreads();
         fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
-        for (int k = tid; k <= half; k += NT) {
+        int j = 0;
+        for (int k = tid; k <= half; k += NT, ++j) {
             const int nk = (k == 0) ? 0 : N - k;
             float2 xk, xnk;
             rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
             const int bnk = N - k;
-            Xs[k] = xk;
-            if (bnk != k) Xs[bnk] = xnk;
+            if (early) {
+                if (j < C::MAXK) { xr[j][0] = xk; xr[j][1] = xnk; }
+            } else {
+                Xs[k] = xk;
+                if (bnk != k) Xs[bnk] = xnk;
+            }
             const float2 pk = cmul(xk, h0s[k]);
             const float2 pnk = cmul(xnk, h0s[bnk]);
             h0s[k] = pk;
@@ -340,10 +346,15 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
 
     if (early) forward_pass();
 
-    // earlier steps' kernels have completed and their writes are visible; the
-    // next step's kernel may now start its own independent part
+    // earlier steps' kernels have completed and their writes are visible
     cudaGridDependencySynchronize();
-    cudaTriggerProgrammaticLaunchCompletion();
+    if (early) {   // X_b, held in registers since the forward pass
+        for (int k = tid, j = 0; k <= half; k += NT, ++j) {
+            const int bnk = N - k;
+            Xs[k] = xr[j][0];
+            if (bnk != k) Xs[bnk] = xr[j][1];
+        }
+    }
 
     if constexpr (C::PREFETCH) {
         // ---- dependent inputs: input-ring history (unless EARLY), previous
@@ -523,9 +534,9 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     __shared__ __align__(16) RunState rs;
     __shared__ int s_last;
     const int tid = threadIdx.x;
-    // The next step's kernel is signalled only after this grid's dependency
-    // wait (in fire_body and below), so its independent part never overlaps
-    // a kernel older than this one.
+    // the next step's CTAs may start their independent part now; they wait in
+    // cudaGridDependencySynchronize() until this grid has completed
+    cudaTriggerProgrammaticLaunchCompletion();
     if (tid < 12) {
         reinterpret_cast<int4*>(&tk)[tid] = __ldg(reinterpret_cast<const int4*>(tasks + blockIdx.x) + tid);
     } else if (tid >= 32 && tid < 37) {
@@ -537,7 +548,6 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     const long long c = rs.step_base + step_in_batch;
     if (tk.kind == 1) {
         cudaGridDependencySynchronize();
-        cudaTriggerProgrammaticLaunchCompletion();
         spread_body<C::NT>(tk, c, dyn_smem);
         return;
     }

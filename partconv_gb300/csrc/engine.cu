@@ -134,7 +134,6 @@ struct pc_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t side[kClasses] = {nullptr, nullptr, nullptr};   // graph-capture branches
     cudaStream_t aside[kClasses] = {nullptr, nullptr, nullptr};  // deferred fires (graph capture)
-    cudaStream_t aspread[kClasses] = {nullptr, nullptr, nullptr};  // their spread tasks
 
     int fs = 0, N0 = 0, n_in = 0, n_out = 0;
     int relaxed = 0;
@@ -160,12 +159,9 @@ struct pc_handle {
     // Deferred fires (levels >= 1 whose output is due more than one step
     // after their block completes): launched after the step that completed
     // the block, on a low-priority stream, and joined `due` steps later.
-    // Each group also carries the spread tasks that build parts >= 2 of its
-    // levels' next blocks (soff/scnt), run beside the fire on a second
-    // low-priority stream.
     struct DGroup {
-        int cls, phase, due, off, cnt, soff, scnt;
-        double bytes, sbytes;
+        int cls, phase, due, off, cnt;
+        double bytes;
     };
     std::vector<DGroup> dgroups;
     std::vector<std::vector<int>> dg_of_phase;   // phase -> indices into dgroups
@@ -227,10 +223,6 @@ void free_device(pc_handle* h) {
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
-    for (auto& s : h->aspread) {
-        if (s) cudaStreamDestroy(s);
-        s = nullptr;
-    }
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     h->ready = false;
@@ -262,12 +254,6 @@ int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool f
            "deferred fire launch");
         first = false;
         h->launches += 1;
-        if (gr.scnt > 0) {
-            CK(launch_step_class(h->l0_class, gr.scnt, h->class_maxN[h->l0_class], h->bank, h->d_tasks + gr.soff, rs,
-                                 nullptr, 0, st, true),
-               "deferred spread launch");
-            h->launches += 1;
-        }
     }
     return PC_OK;
 }
@@ -292,7 +278,6 @@ int build_graph(pc_handle* h) {
         cudaEvent_t done;
     };
     std::vector<Pending> pending;   // deferred fires in flight
-    cudaEvent_t spread_done[kClasses] = {nullptr, nullptr, nullptr};   // latest spread launch per class
     for (int s = 0; s < h->G && e == cudaSuccess; ++s) {
         const int ph = s & (h->H - 1);
         // deferred fires whose output this step emits join the chain here
@@ -332,11 +317,7 @@ int build_graph(pc_handle* h) {
             const pc_handle::DGroup& gr = h->dgroups[gi];
             cudaEvent_t fork = mk();
             e = cudaEventRecord(fork, h->stream);
-            // the fire reads the partial sums built by the spread launched with
-            // its level's previous fire: the latest of its class or an older one
             if (e == cudaSuccess) e = cudaStreamWaitEvent(h->aside[gr.cls], fork, 0);
-            if (e == cudaSuccess && spread_done[gr.cls])
-                e = cudaStreamWaitEvent(h->aside[gr.cls], spread_done[gr.cls], 0);
             if (e == cudaSuccess)
                 e = launch_step_class(gr.cls, gr.cnt, h->class_maxN[gr.cls], h->bank, h->d_tasks + gr.off, dummy,
                                       h->d_rs, s, h->aside[gr.cls], false, -1);
@@ -344,26 +325,12 @@ int build_graph(pc_handle* h) {
             if (e == cudaSuccess) e = cudaEventRecord(done, h->aside[gr.cls]);
             pending.push_back({s + gr.due, done});
             ++kernels;
-            // parts >= 2 of the next blocks: spectra of fires joined before this
-            // step, into the other half of the partial-sum buffers
-            if (gr.scnt > 0 && e == cudaSuccess) {
-                e = cudaStreamWaitEvent(h->aspread[gr.cls], fork, 0);
-                if (e == cudaSuccess)
-                    e = launch_step_class(h->l0_class, gr.scnt, h->class_maxN[h->l0_class], h->bank,
-                                          h->d_tasks + gr.soff, dummy, h->d_rs, s, h->aspread[gr.cls], false, -1);
-                cudaEvent_t sd = mk();
-                if (e == cudaSuccess) e = cudaEventRecord(sd, h->aspread[gr.cls]);
-                spread_done[gr.cls] = sd;
-                ++kernels;
-            }
         }
     }
-    // the graph ends with every deferred fire and spread joined (a replay
-    // must not overlap the next one's state update)
+    // the graph ends with every deferred fire joined (a replay must not
+    // overlap the next one's state update)
     for (auto& pd : pending)
         if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, pd.done, 0);
-    for (auto sd : spread_done)
-        if (sd && e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, sd, 0);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     for (auto ev : evs) cudaEventDestroy(ev);
     if (e == cudaSuccess) e = e2;
@@ -398,7 +365,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     CK(cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_greatest), "stream create");
     for (auto& s : h->side) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_greatest), "stream create");
     for (auto& s : h->aside) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_least), "stream create");
-    for (auto& s : h->aspread) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_least), "stream create");
     CK(prepare_kernels(), "kernel attributes");
 
     h->fs = fs;
@@ -538,8 +504,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     std::vector<std::vector<std::vector<Task>>> lists(kClasses, std::vector<std::vector<Task>>(Hh));
     std::map<std::tuple<int, int, int>, std::vector<Task>> dlists;   // (phase, due, class) -> deferred fires
     std::map<std::tuple<int, int, int>, double> dbytes;
-    std::map<std::tuple<int, int, int>, std::vector<Task>> dspreads;   // their spread tasks
-    std::map<std::tuple<int, int, int>, double> dsbytes;
     for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(Hh, 0.0);
     // order: larger fires first (longest CTAs start first), then level-0
     // fires, then spread tasks
@@ -584,29 +548,9 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 b += 8.0 * C;
             }
             if (dwin[li] > 0) {
-                const auto key = std::make_tuple(g, dwin[li] + 1, cls);
                 t.dfer = 1;
-                dlists[key].push_back(t);
-                dbytes[key] += b;
-                // parts >= 2 of the level's next block, all bins
-                if (l.P >= 3) {
-                    for (int k0 = 0; k0 < l.cs; k0 += spread_task_bins()) {
-                        Task u{};
-                        u.kind = 1;
-                        u.N = l.N;
-                        u.P = l.P;
-                        u.T = l.T;
-                        u.s_blocks = l.s_blocks;
-                        u.cs = l.cs;
-                        u.k0 = k0;
-                        u.k1 = std::min(l.cs, k0 + spread_task_bins());
-                        u.p_lo = 2;
-                        u.lv_index = li;
-                        u.dfer = 1;
-                        dspreads[key].push_back(u);
-                    }
-                    dsbytes[key] += (16.0 * (l.P - 2) + 8.0) * l.cs;
-                }
+                dlists[std::make_tuple(g, dwin[li] + 1, cls)].push_back(t);
+                dbytes[std::make_tuple(g, dwin[li] + 1, cls)] += b;
                 continue;
             }
             lists[cls][g].push_back(t);
@@ -622,7 +566,14 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 hi = l.cs;
                 p_lo = 2;
             } else if (dwin[li] > 0) {
-                continue;   // built beside the level's deferred fire
+                // parts >= 2 of the next deferred fire, in T slices over all
+                // phases (the fire's own step builds the last slice)
+                if (l.P < 3) continue;
+                const int phi = (g + 1 + l.s_blocks) % l.T;
+                const int j = (phi + l.T - 1) % l.T, nch = l.T;
+                lo = (int)(((long)j * l.cs / nch) & ~1L);
+                hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
+                p_lo = 2;
             } else {
                 if (l.P < 2) continue;
                 const int phi = (g + 1 + l.s_blocks) % l.T;
@@ -644,6 +595,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 t.k1 = std::min(hi, k0 + spread_task_bins());
                 t.p_lo = p_lo;
                 t.lv_index = li;
+                t.dfer = dwin[li] > 0;
                 lists[sc][g].push_back(t);
             }
             h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0) * (hi - lo);
@@ -670,14 +622,9 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         gr.off = (int)ntasks;
         gr.cnt = (int)kv.second.size();
         gr.bytes = dbytes[kv.first];
-        ntasks += kv.second.size();
-        const auto& sp = dspreads[kv.first];
-        gr.soff = (int)ntasks;
-        gr.scnt = (int)sp.size();
-        gr.sbytes = dsbytes[kv.first];
-        ntasks += sp.size();
         h->dg_of_phase[gr.phase].push_back((int)h->dgroups.size());
         h->dgroups.push_back(gr);
+        ntasks += kv.second.size();
     }
     const size_t off_tasks = cv.take(sizeof(Task) * std::max<size_t>(1, ntasks));
 
@@ -731,10 +678,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     std::vector<const std::vector<Task>*> in_order;
     for (int cls = 0; cls < kClasses; ++cls)
         for (int g = 0; g < Hh; ++g) in_order.push_back(&lists[cls][g]);
-    for (auto& kv : dlists) {
-        in_order.push_back(&kv.second);
-        in_order.push_back(&dspreads[kv.first]);
-    }
+    for (auto& kv : dlists) in_order.push_back(&kv.second);
     for (const auto* lst : in_order)
             for (Task t : *lst) {
                 const DevLevel& l = h->h_lv[t.lv_index];
@@ -1218,8 +1162,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     struct Rec {
         int cls;
         int phase;
-        int dgroup;    // -1: the class's per-phase list
-        bool spread;   // the deferred group's spread launch
+        int dgroup;   // -1: the class's per-phase list
         cudaEvent_t a, b;
     };
     std::vector<Rec> recs;
@@ -1237,7 +1180,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
             const int cls = (h->l0_class + k) % kClasses;
             const int n = h->cnt[cls][ph];
             if (n <= 0) continue;
-            Rec r{cls, ph, -1, false, nullptr, nullptr};
+            Rec r{cls, ph, -1, nullptr, nullptr};
             cudaEventCreate(&r.a);
             cudaEventCreate(&r.b);
             cudaEventRecord(r.a, h->stream);
@@ -1251,7 +1194,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
         for (int gi : h->dg_of_phase[ph]) {
             if (rc != PC_OK) break;
             const pc_handle::DGroup& gr = h->dgroups[gi];
-            Rec r{gr.cls, ph, gi, false, nullptr, nullptr};
+            Rec r{gr.cls, ph, gi, nullptr, nullptr};
             cudaEventCreate(&r.a);
             cudaEventCreate(&r.b);
             cudaEventRecord(r.a, h->stream);
@@ -1259,17 +1202,6 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
                                               nullptr, 0, h->stream, false);
             cudaEventRecord(r.b, h->stream);
             recs.push_back(r);
-            h->launches += 1;
-            if (e != cudaSuccess) rc = cuda_fail(h, e, "profile launch");
-            if (gr.scnt <= 0 || rc != PC_OK) continue;
-            Rec q{h->l0_class, ph, gi, true, nullptr, nullptr};
-            cudaEventCreate(&q.a);
-            cudaEventCreate(&q.b);
-            cudaEventRecord(q.a, h->stream);
-            e = launch_step_class(h->l0_class, gr.scnt, h->class_maxN[h->l0_class], h->bank, h->d_tasks + gr.soff, rs,
-                                  nullptr, 0, h->stream, false);
-            cudaEventRecord(q.b, h->stream);
-            recs.push_back(q);
             h->launches += 1;
             if (e != cudaSuccess) rc = cuda_fail(h, e, "profile launch");
         }
@@ -1282,8 +1214,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
         float t = 0.f;
         if (se == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
             ms[r.cls] += t;
-            bytes[r.cls] += r.dgroup < 0 ? h->alg_bytes[r.cls][r.phase]
-                                         : (r.spread ? h->dgroups[r.dgroup].sbytes : h->dgroups[r.dgroup].bytes);
+            bytes[r.cls] += r.dgroup < 0 ? h->alg_bytes[r.cls][r.phase] : h->dgroups[r.dgroup].bytes;
             cnt[r.cls] += 1;
         }
         cudaEventDestroy(r.a);

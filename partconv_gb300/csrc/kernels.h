@@ -29,9 +29,12 @@ size_t class_smem_bytes(int cls, int maxN);
 cudaError_t prepare_kernels();
 // pdl: let the launch overlap the previous kernel in the stream, which must
 // be a step kernel of the same handle (or nothing)
-// prio: 0 = the stream's priority, 1 = the device's highest, -1 = its lowest
+// prio: 0 = the stream's priority, 1 = the device's highest, -1 = its lowest.
+// whole_sm: request enough shared memory that no other CTA fits beside one
+// of these (classes 1 and 2).
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
-                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio = 0);
+                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio = 0,
+                              bool whole_sm = false);
 cudaError_t launch_pool_class(int cls, int grid, int maxN, const Bank& bank, const Task* slots, const PoolCta* map,
                               const RunState& rs, cudaStream_t st);
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,

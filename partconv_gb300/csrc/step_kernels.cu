@@ -30,6 +30,8 @@
 // only then uses them (one memory round trip per phase).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "engine_types.h"
 #include "fft_smem.cuh"
 #include "kernels.h"
@@ -68,6 +70,9 @@ struct Cls {
     static constexpr int SPLIT_CH = 4;                           // post-FFT pairs loaded per batch
     static_assert(MAXB >= 1, "class too small");
 };
+// dynamic shared memory that leaves no room for a level-0 CTA beside it on
+// an SM (228 KB per SM, 1 KB reserved per CTA, 227 KB per CTA at most)
+constexpr size_t kWholeSmSmem = 220 * 1024;
 using Cls0 = Cls<256, 1024, true>;
 using Cls1 = Cls<512, 4096, false>;
 using Cls2 = Cls<512, 16384, false>;
@@ -685,10 +690,10 @@ cudaError_t prepare_kernels() {
                              (int)class_smem_bytes(0, Cls0::MAXN));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(step_kernel<Cls1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)class_smem_bytes(1, Cls1::MAXN));
+                             (int)std::max(class_smem_bytes(1, Cls1::MAXN), kWholeSmSmem));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(step_kernel<Cls2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)class_smem_bytes(2, Cls2::MAXN));
+                             (int)std::max(class_smem_bytes(2, Cls2::MAXN), kWholeSmSmem));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(spectra_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(12 * 16384));
@@ -705,7 +710,8 @@ cudaError_t prepare_kernels() {
 }
 
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
-                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio) {
+                              const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio,
+                              bool whole_sm) {
     if (grid <= 0) return cudaSuccess;
     static int least = 0, greatest = 0;
     static const bool have_range = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess;
@@ -731,6 +737,7 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kNT[cls]);
     cfg.dynamicSmemBytes = class_smem_bytes(cls, maxN);
+    if (whole_sm && cls != 0) cfg.dynamicSmemBytes = std::max(cfg.dynamicSmemBytes, kWholeSmSmem);
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = na;

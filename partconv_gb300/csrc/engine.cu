@@ -134,7 +134,6 @@ struct pc_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t side[kClasses] = {nullptr, nullptr, nullptr};   // graph-capture branches
     cudaStream_t aside[kClasses] = {nullptr, nullptr, nullptr};  // deferred fires (graph capture)
-    cudaStream_t sside = nullptr;                                  // per-step spread tasks (graph capture)
 
     int fs = 0, N0 = 0, n_in = 0, n_out = 0;
     int relaxed = 0;
@@ -156,7 +155,6 @@ struct pc_handle {
     // per (class, phase) task lists: d_tasks + off[cls][phase], count cnt[cls][phase]
     Task* d_tasks = nullptr;
     std::vector<int> off[kClasses], cnt[kClasses];
-    std::vector<int> nfire;   // level-0 class, per phase: fire tasks first, then spread tasks
     std::vector<double> alg_bytes[kClasses];
     // Deferred fires (levels >= 1 whose output is due more than one step
     // after their block completes): launched after the step that completed
@@ -225,8 +223,6 @@ void free_device(pc_handle* h) {
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
-    if (h->sside) cudaStreamDestroy(h->sside);
-    h->sside = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     h->ready = false;
@@ -282,7 +278,6 @@ int build_graph(pc_handle* h) {
         cudaEvent_t done;
     };
     std::vector<Pending> pending;   // deferred fires in flight
-    cudaEvent_t spread_done = nullptr;   // the previous step's spread tasks
     for (int s = 0; s < h->G && e == cudaSuccess; ++s) {
         const int ph = s & (h->H - 1);
         // deferred fires whose output this step emits join the chain here
@@ -293,26 +288,6 @@ int build_graph(pc_handle* h) {
             } else {
                 ++i;
             }
-        }
-        // this step's fires read the partial sums the previous step's spread
-        // tasks built
-        if (spread_done && e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, spread_done, 0);
-        spread_done = nullptr;
-        // Spread tasks (partial sums for later fires) read only spectra of
-        // fires that have completed, so they run beside this step's fires
-        // instead of lengthening the level-0 kernel.
-        const int c0s = h->l0_class;
-        const int nsp = h->cnt[c0s][ph] - h->nfire[ph];
-        if (nsp > 0 && e == cudaSuccess) {
-            cudaEvent_t fork = mk();
-            e = cudaEventRecord(fork, h->stream);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->sside, fork, 0);
-            if (e == cudaSuccess)
-                e = launch_step_class(c0s, nsp, h->class_maxN[c0s], h->bank, h->d_tasks + h->off[c0s][ph] + h->nfire[ph],
-                                      dummy, h->d_rs, s, h->sside, false);
-            spread_done = mk();
-            if (e == cudaSuccess) e = cudaEventRecord(spread_done, h->sside);
-            ++kernels;
         }
         std::vector<cudaEvent_t> joins;
         for (int cls = 0; cls < kClasses && e == cudaSuccess; ++cls) {
@@ -330,7 +305,7 @@ int build_graph(pc_handle* h) {
         }
         const int c0 = h->l0_class;
         if (e == cudaSuccess)
-            e = launch_step_class(c0, h->nfire[ph], h->class_maxN[c0], h->bank, h->d_tasks + h->off[c0][ph], dummy,
+            e = launch_step_class(c0, h->cnt[c0][ph], h->class_maxN[c0], h->bank, h->d_tasks + h->off[c0][ph], dummy,
                                   h->d_rs, s, h->stream, s > 0, 1);
         ++kernels;
         for (auto j : joins)
@@ -358,7 +333,6 @@ int build_graph(pc_handle* h) {
     // overlap the next one's state update)
     for (auto& pd : pending)
         if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, pd.done, 0);
-    if (spread_done && e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, spread_done, 0);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     for (auto ev : evs) cudaEventDestroy(ev);
     if (e == cudaSuccess) e = e2;
@@ -393,7 +367,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     CK(cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_greatest), "stream create");
     for (auto& s : h->side) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_greatest), "stream create");
     for (auto& s : h->aside) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_least), "stream create");
-    CK(cudaStreamCreateWithPriority(&h->sside, cudaStreamNonBlocking, prio_greatest), "stream create");
     CK(prepare_kernels(), "kernel attributes");
 
     h->fs = fs;
@@ -534,7 +507,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     std::map<std::tuple<int, int, int>, std::vector<Task>> dlists;   // (phase, due, class) -> deferred fires
     std::map<std::tuple<int, int, int>, double> dbytes;
     for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(Hh, 0.0);
-    h->nfire.assign(Hh, 0);
     // order: larger fires first (longest CTAs start first), then level-0
     // fires, then spread tasks
     std::vector<int> order(nlv);
@@ -587,7 +559,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             h->alg_bytes[cls][g] += b;
         }
         const int sc = h->l0_class;
-        h->nfire[g] = (int)lists[sc][g].size();
         for (int li = 0; li < nlv; ++li) {
             const DevLevel& l = h->h_lv[li];
             int lo, hi, p_lo;

@@ -164,3 +164,97 @@ def choose_layout(ir_len: int, N0: int, batch: int = 32, cache: str | None = DEF
                     json.dump(cur, f, indent=1, sort_keys=True)
                 os.replace(tmp, cache)
     return _fit(db[key]["best"]["N"], db[key]["best"]["P"], ir_len)
+
+
+# ---------------------------------------------------------------------------
+# Dynamic program over level costs (matlab/optimal_part.m's Viterbi search,
+# restated over levels instead of block positions).
+# ---------------------------------------------------------------------------
+def model_level_cost(N: int, P: int, N0: int, k: float = 1.5) -> float:
+    """Cost per base step of a level of block N with P parts under the
+    reference's model (matlab/optimal_part.m: 4 k log2(2N) + 4 per new block
+    size, 4 per part), amortised over the N / N0 base steps of one block."""
+    return (4.0 * k * np.log2(2 * N) + 4.0 * P) * N0 / N
+
+
+def optimal_part(ir_len: int, N0: int, level_cost=None, max_block: int = 16384, strict: bool = False):
+    """Layout (N, P) minimising the sum of level_cost(N, P, N0) over levels.
+
+    Levels have power-of-two blocks growing from N0 (any factor), and each
+    level L >= 1 must satisfy the delay rule for its offset s_L (relaxed:
+    s_L >= N_L; strict: 2 N0 + s_L >= 2 N_L).  States are (block size,
+    taps covered) in units of N0; the last level's part count covers the
+    rest of the IR.  level_cost defaults to model_level_cost; pass
+    measured_level_costs(...) for GPU timings."""
+    cost = level_cost or model_level_cost
+    U = -(-int(ir_len) // N0)                      # IR length in base blocks
+    sizes = []
+    n = N0
+    while n <= max_block:
+        sizes.append(n)
+        n *= 2
+    best = {}                                      # (size index, covered) -> (cost, parent, parts)
+
+    def ok(Ni, covered):                           # delay rule for a new level of block Ni at offset covered
+        s = covered * N0
+        return (2 * N0 + s >= 2 * Ni) if strict else (s >= Ni)
+
+    # level 0: P parts of N0
+    for P in range(1, U + 1):
+        best[(0, P)] = (cost(N0, P, N0), None, P)
+    result = None
+    for i in range(len(sizes)):
+        for cov in sorted(c for (j, c) in list(best) if j == i):
+            cst, _, _ = best[(i, cov)]
+            if cov >= U:
+                if result is None or cst < result[0]:
+                    result = (cst, (i, cov))
+                continue
+            for j in range(i + 1, len(sizes)):
+                Nj = sizes[j]
+                if not ok(Nj, cov):
+                    continue
+                b = Nj // N0
+                maxP = -(-(U - cov) // b)
+                for P in range(1, maxP + 1):
+                    key = (j, cov + P * b) if P < maxP else (j, U)
+                    v = cst + cost(Nj, P, N0)
+                    if key not in best or v < best[key][0]:
+                        best[key] = (v, (i, cov), P)
+    if result is None:
+        raise ValueError("no valid layout")
+    N, P = [], []
+    key = result[1]
+    while key is not None:
+        _, parent, parts = best[key]
+        N.append(sizes[key[0]])
+        P.append(parts)
+        key = parent
+    return N[::-1], P[::-1]
+
+
+def measured_level_costs(N0: int, sizes=None, parts=(2, 8), trials: int = 200):
+    """level_cost(N, P, N0) from GPU timings: PartConvFilter.bench of one
+    level (device time per block, CUDA events) at two part counts, fitted
+    as a + b P per block and amortised over the N / N0 base steps."""
+    from . import partconv
+
+    sizes = sizes or [N0 << j for j in range(8) if (N0 << j) <= 16384]
+    fit = {}
+    for N in sizes:
+        ts = []
+        for P in parts:
+            f = partconv.PartConvFilter()
+            Na, Pa = partconv.intArray(1), partconv.intArray(1)
+            Na[0], Pa[0] = N, P
+            if f.setup(1, Na, Pa, None) != 0:
+                raise RuntimeError(f.last_error)
+            ts.append(f.bench(0, trials, 0, 0.1))
+            f.cleanup()
+        b = max((ts[1] - ts[0]) / (parts[1] - parts[0]), 1e-12)   # timing noise must not make parts free
+        fit[N] = (max(ts[0] - b * parts[0], 0.0), b)
+
+    def cost(N, P, n0=N0):
+        a, b = fit[N]
+        return (a + b * P) * n0 / N
+    return cost

@@ -45,3 +45,54 @@ def test_autotuner_measures_and_caches(gpu, tmp_path):
     assert rec["best"]["us_per_step"] == min(c["us_per_step"] for c in rec["candidates"])
     # a second call is served from the cache
     assert autotune.choose_layout(20000, 256, batch=8, cache=cache) == (N, P)
+
+
+def _brute_chain(L, N0, strict, cost):
+    sizes = [N0 << j for j in range(6)]
+    U = -(-L // N0)
+    best = [None]
+
+    def rec(N, P, cov, c):
+        if cov >= U:
+            if best[0] is None or c < best[0][0]:
+                best[0] = (c, list(N), list(P))
+            return
+        for Nj in sizes:
+            if (N and Nj <= N[-1]) or (not N and Nj != N0):
+                continue
+            if N and ((2 * N0 + cov * N0 < 2 * Nj) if strict else (cov * N0 < Nj)):
+                continue
+            b = Nj // N0
+            for p in range(1, -(-(U - cov) // b) + 1):
+                rec(N + [Nj], P + [p], min(U, cov + p * b), c + cost(Nj, p, N0))
+
+    rec([], [], 0, 0.0)
+    return best[0]
+
+
+@pytest.mark.parametrize("L,N0,strict", [(3000, 64, False), (5000, 64, True), (1200, 32, False), (9000, 128, False),
+                                         (700, 16, True)])
+def test_optimal_part_dp_matches_exhaustive_search(L, N0, strict):
+    """The level DP (matlab/optimal_part.m's search, over levels) finds the
+    cheapest valid chain under the reference's cost model."""
+    from partconv_gb300 import autotune as at
+    from partconv_gb300.multi import check_layout
+
+    N, P = at.optimal_part(L, N0, strict=strict)
+    c = sum(at.model_level_cost(n, p, N0) for n, p in zip(N, P))
+    want = _brute_chain(L, N0, strict, at.model_level_cost)
+    assert c == pytest.approx(want[0], rel=1e-12)
+    st, _, _, msg = check_layout(N, P, L, relaxed=not strict)
+    assert st == 0, msg
+
+
+@pytest.mark.gpu
+def test_optimal_part_on_measured_costs(gpu):
+    from partconv_gb300 import autotune as at
+    from partconv_gb300.multi import check_layout
+
+    cost = at.measured_level_costs(256, sizes=[256, 512, 1024, 2048, 4096], trials=50)
+    N, P = at.optimal_part(40000, 256, cost, max_block=4096)
+    st, _, _, msg = check_layout(N, P, 40000)
+    assert st == 0, msg
+    assert all(cost(n, p) > 0 for n, p in zip(N, P))

@@ -139,6 +139,86 @@ __device__ void fft_smem(float2* s, int N, int logN, const Twiddles& tw, bool in
     if (lgNs < logN) stage_r2<NT, MAXB>(s, N, Ns, lgNs, tw, inv);
 }
 
+// Radix-4 and radix-2 Stockham stages from src to dst (a second buffer): one
+// barrier per stage instead of two, and the same arithmetic as the in-place
+// stages, so results are bit-identical.
+template <int NT, int MAXB>
+__device__ __forceinline__ void stage_r4_pp(const float2* src, float2* dst, int N, int Ns, int lgNs,
+                                            const Twiddles& tw, bool inv) {
+    const int nb = N >> 2;
+#pragma unroll
+    for (int i = 0; i < MAXB; ++i) {
+        const int j = threadIdx.x + i * NT;
+        if (j < nb) {
+            float2 v[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) v[r] = src[j + r * nb];
+            const int k = j & (Ns - 1);
+            if (Ns > 1) {
+                const int lg = lgNs + 2;
+                v[1] = cmul(v[1], tw.get(k, lg, inv));
+                v[2] = cmul(v[2], tw.get(2 * k, lg, inv));
+                v[3] = cmul(v[3], tw.get(3 * k, lg, inv));
+            }
+            const float2 a0 = cadd(v[0], v[2]);
+            const float2 a1 = csub(v[0], v[2]);
+            const float2 a2 = cadd(v[1], v[3]);
+            const float2 d = csub(v[1], v[3]);
+            const float2 a3 = inv ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+            const int base = ((j - k) << 2) + k;
+            dst[base] = cadd(a0, a2);
+            dst[base + Ns] = cadd(a1, a3);
+            dst[base + 2 * Ns] = csub(a0, a2);
+            dst[base + 3 * Ns] = csub(a1, a3);
+        }
+    }
+    __syncthreads();
+}
+
+template <int NT, int MAXB>
+__device__ __forceinline__ void stage_r2_pp(const float2* src, float2* dst, int N, int Ns, int lgNs,
+                                            const Twiddles& tw, bool inv) {
+    const int nb = N >> 1;
+#pragma unroll
+    for (int i = 0; i < 2 * MAXB; ++i) {
+        const int j = threadIdx.x + i * NT;
+        if (j < nb) {
+            const float2 v0 = src[j];
+            float2 b = src[j + nb];
+            const int k = j & (Ns - 1);
+            if (Ns > 1) b = cmul(b, tw.get(k, lgNs + 1, inv));
+            const int base = ((j - k) << 1) + k;
+            dst[base] = cadd(v0, b);
+            dst[base + Ns] = csub(v0, b);
+        }
+    }
+    __syncthreads();
+}
+
+// fft_smem with a scratch buffer tmp of N points: stages alternate between
+// s and tmp (the first one runs in place when the stage count is odd), so
+// the result ends in s.  Same preconditions and results as fft_smem.
+template <int NT, int MAXB>
+__device__ void fft_smem_pp(float2* s, float2* tmp, int N, int logN, const Twiddles& tw, bool inv) {
+    const int n4 = logN >> 1, n2 = logN & 1;
+    int Ns = 1, lgNs = 0, st = 0;
+    float2* a = s;
+    float2* b = tmp;
+    if ((n4 + n2) & 1) {   // odd stage count: one in-place stage first
+        stage_r4<NT, MAXB>(s, N, Ns, lgNs, tw, inv);
+        lgNs += 2;
+        Ns <<= 2;
+        st = 1;
+    }
+    for (; st < n4; ++st, lgNs += 2, Ns <<= 2) {
+        stage_r4_pp<NT, MAXB>(a, b, N, Ns, lgNs, tw, inv);
+        float2* t = a;
+        a = b;
+        b = t;
+    }
+    if (n2) stage_r2_pp<NT, MAXB>(a, b, N, Ns, lgNs, tw, inv);
+}
+
 // Split post-pass for the pair (k, N-k), 0 <= k <= N/2, on Z = FFT_N(z).
 // Returns X[k] in xk and X[N-k] in xnk (for k == 0: X[0] and X[N]).
 __device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int logN, const Twiddles& tw, float2& xk,

@@ -79,8 +79,9 @@ using Cls2 = Cls<512, 16384, false>;
 
 // dynamic shared memory bytes of a fire for block size N
 __host__ __device__ constexpr size_t fire_smem_bytes(int N, bool prefetch) {
-    // data N + quarter twiddles N/2 complex (+ yacc N+2, h0 N+2 complex, emit N floats)
-    return prefetch ? (size_t)8 * N + 4 * N + 16 * ((size_t)N + 2) + 4 * (size_t)N
+    // data N + quarter twiddles N/2 complex (+ yacc N+2, h0 N+2 complex, emit N
+    // floats, FFT scratch N complex)
+    return prefetch ? (size_t)8 * N + 4 * N + 16 * ((size_t)N + 2) + 4 * (size_t)N + 8 * (size_t)N
                     : (size_t)8 * N + 4 * (size_t)N;
 }
 
@@ -176,7 +177,13 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     float2* yacc = twt + N / 2;       // N + 2 (PREFETCH)
     float2* h0s = yacc + (N + 2);     // N + 2 (PREFETCH)
     float* emit = reinterpret_cast<float*>(h0s + (N + 2));   // N0 floats (PREFETCH, level 0)
+    float2* ftmp = reinterpret_cast<float2*>(emit + N);       // N complex FFT scratch (PREFETCH)
     const Twiddles tw{twt, logN};
+    // prefetch classes transform through the scratch buffer (fewer barriers)
+    auto fft = [&](bool inv) {
+        if constexpr (C::PREFETCH) fft_smem_pp<NT, C::MAXB>(s, ftmp, N, logN, tw, inv);
+        else fft_smem<NT, C::MAXB>(s, N, logN, tw, inv);
+    };
 
     const long long io_step = c - rs.io.step0;   // I/O is addressed by the global step
     c -= tk.origin;                              // schedule and rings by the PC's own steps
@@ -233,7 +240,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     //      The input-ring append and the other levels' output slices wait for
     //      the dependency (a larger level of the same kernel class may still
     //      be reading the ring and writing its output in the previous step).
-    float4 wv[C::MAXQ];
+    float4 wv[C::MAXQ];   // this step's input quads (kept for the EARLY ring append)
     {
 #pragma unroll
         for (int i = 0; i < C::MAXQ; ++i) {
@@ -300,10 +307,11 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     // parked in shared memory, whether or not the forward transform ran
     // before the dependency wait: one sequence of float operations, so the
     // EARLY and the in-order paths give identical bits.
-    float2 xr[C::MAXK][2];   // EARLY: this thread's X_b pairs until after the wait
+    constexpr int kXr = C::PREFETCH ? C::MAXK : 1;
+    float2 xr[kXr][2];   // EARLY: this thread's X_b pairs until after the wait
     auto forward_pass = [&]() {   // forward FFT, X_b, X_b H_0 -> h0s (k = half: N - k product in slot N + 1)
         __syncthreads();
-        fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
+        fft(false);
         int j = 0;
         for (int k = tid; k <= half; k += NT, ++j) {
             const int nk = (k == 0) ? 0 : N - k;
@@ -311,7 +319,10 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
             const int bnk = N - k;
             if (early) {
-                if (j < C::MAXK) { xr[j][0] = xk; xr[j][1] = xnk; }
+                if (j < kXr) {
+                    xr[j][0] = xk;
+                    xr[j][1] = xnk;
+                }
             } else {
                 Xs[k] = xk;
                 if (bnk != k) Xs[bnk] = xnk;
@@ -474,7 +485,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         __syncthreads();
     }
 
-    fft_smem<NT, C::MAXB>(s, N, logN, tw, true);
+    fft(true);
 
     const float* sf = reinterpret_cast<const float*>(s);   // y[i] = sf[i], i < 2N
     if (!l0) {

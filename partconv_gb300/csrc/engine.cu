@@ -495,6 +495,11 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 l.cs = p.N[L] + 2;
                 l.rmask = rl[li] - 1;
                 l.pc = i;
+                {   // spread tasks sum parts >= 2 (level 0, deferred levels) or >= 1
+                    const int p_lo = (L == 0 || dwin[li] > 0) ? 2 : 1;
+                    const int np = p.P[L] - p_lo;
+                    l.npart = np > 0 ? (np + spread_task_parts() - 1) / spread_task_parts() : 1;
+                }
                 s += (long)p.N[L] * p.P[L];
             }
         }
@@ -544,11 +549,12 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             const double C = l.N + 1.0;
             double b = 8.0 * C * 2.0 + 12.0 * l.N;
             if (l.T == 1 || dwin[li] > 0) {
-                b += 8.0 * C * (l.P >= 2 ? 2.0 : 0.0) + (l.P >= 3 ? 8.0 * C : 0.0);
+                b += 8.0 * C * (l.P >= 2 ? 2.0 : 0.0) + (l.P >= 3 ? 8.0 * C * l.npart : 0.0);
                 if (l.T == 1) b += 4.0 * N0 * (d.M - 1) + 4.0 * N0;
             } else if (l.P >= 2) {
-                b += 8.0 * C;
+                b += 8.0 * C * l.npart;
             }
+            t.k0 = l.npart;   // partial-sum rows the fire adds
             if (dwin[li] > 0) {
                 t.dfer = 1;
                 dlists[std::make_tuple(g, dwin[li] + 1, cls)].push_back(t);
@@ -585,22 +591,25 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
                 p_lo = 1;
             }
-            for (int k0 = lo; k0 < hi; k0 += spread_task_bins()) {
-                Task t{};
-                t.kind = 1;
-                t.N = l.N;
-                t.P = l.P;
-                t.T = l.T;
-                t.s_blocks = l.s_blocks;
-                t.cs = l.cs;
-                t.k0 = k0;
-                t.k1 = std::min(hi, k0 + spread_task_bins());
-                t.p_lo = p_lo;
-                t.lv_index = li;
-                t.dfer = dwin[li] > 0;
-                lists[sc][g].push_back(t);
-            }
-            h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0) * (hi - lo);
+            for (int k0 = lo; k0 < hi; k0 += spread_task_bins())
+                for (int r = 0; r < l.npart; ++r) {   // parts [p_lo + 16 r, p_lo + 16 (r + 1)) into row r
+                    Task t{};
+                    t.kind = 1;
+                    t.N = l.N;
+                    t.P = l.P;
+                    t.T = l.T;
+                    t.s_blocks = l.s_blocks;
+                    t.cs = l.cs;
+                    t.k0 = k0;
+                    t.k1 = std::min(hi, k0 + spread_task_bins());
+                    t.p_lo = p_lo + r * spread_task_parts();
+                    t.in_ch = std::min(l.P, p_lo + (r + 1) * spread_task_parts());
+                    t.out_ch = r;
+                    t.lv_index = li;
+                    t.dfer = dwin[li] > 0;
+                    lists[sc][g].push_back(t);
+                }
+            h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0 * l.npart) * (hi - lo);
         }
     }
     size_t ntasks = 0;
@@ -644,7 +653,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     for (int li = 0; li < nlv; ++li) {
         const DevLevel& l = h->h_lv[li];
         so.X[li] = cv.take(sizeof(float2) * (size_t)l.P * l.cs);
-        so.Yp[li] = cv.take(sizeof(float2) * 2 * (size_t)l.cs);
+        so.Yp[li] = cv.take(sizeof(float2) * 2 * (size_t)l.npart * l.cs);
         so.yr[li] = cv.take(sizeof(float) * (size_t)(l.rmask + 1));
     }
     so.mix = cv.take(sizeof(int) * n_out);

@@ -30,9 +30,10 @@ struct DevLevel {
     int cs;         // row stride in complex values (N_L + 2)
     int rmask;      // output ring size - 1 (levels >= 1)
     int pc;         // owning PC
+    int npart;      // partial-sum rows (spread tasks cover at most kSpreadParts parts each)
     float2* H;      // [P][cs]
     float2* X;      // [P][cs]
-    float2* Yp;     // [2][cs]
+    float2* Yp;     // [npart][2][cs]: row q, block parity
     float* yring;   // [rmask + 1]
 };
 
@@ -54,8 +55,10 @@ struct DevPC {
 
 // A unit of work of one base step, self-contained so a CTA needs one load
 // to start.  kind 0 (fire): compute one level block -- window, FFT, MAC,
-// inverse FFT, output (level 0 also emits the step's output).  kind 1
-// (spread): partial FDL MAC over bins [k0, k1) for a level's next block.
+// inverse FFT, output (level 0 also emits the step's output); k0 holds the
+// number of partial-sum rows to add (0 means 1).  kind 1 (spread): partial
+// FDL MAC over bins [k0, k1) and parts [p_lo, in_ch) (in_ch 0: up to P) of
+// a level's next block, written to partial-sum row out_ch.
 struct Task {
     int kind, N, logN, P;
     int T, s_blocks, cs, rmask;

@@ -24,6 +24,7 @@ int fire_class_of(int N);
 int class_threads(int cls);
 // bins one spread task covers
 int spread_task_bins();
+int spread_task_parts();
 size_t class_smem_bytes(int cls, int maxN);
 
 cudaError_t prepare_kernels();

@@ -90,6 +90,8 @@ __host__ __device__ constexpr size_t fire_smem_bytes(int N, bool prefetch) {
 // group g sums parts p_lo + g, p_lo + g + G, ...; groups are added in order.
 // ---------------------------------------------------------------------------
 constexpr int kSpreadLanes = 64;   // threads per part-group: a task covers 128 bins
+// parts per spread task: one round of loads (4 groups x 4 in flight) per CTA
+constexpr int kSpreadParts = 16;
 
 template <int NT>
 __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4* red) {
@@ -101,15 +103,17 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
     long long bt;      // block whose partial sum this step builds
     float2* dst;
     c -= tk.origin;    // the PC's own step count
+    const size_t row = (size_t)tk.out_ch * 2;   // partial-sum row, [row][parity][cs]
     if (tk.T == 1) {   // level 0: parts p >= 2 of block c + 1
         bt = c + 1;
-        dst = tk.Yp + (size_t)(bt & 1) * tk.cs;
+        dst = tk.Yp + (row + (size_t)(bt & 1)) * tk.cs;
     } else {           // the block after the newest fired one: parts p >= 1, or
                        // p >= 2 (double-buffered) for a deferred level
         bt = (c + 1 + tk.s_blocks) / tk.T;
-        dst = tk.Yp + (tk.dfer ? (size_t)(bt & 1) * tk.cs : 0);
+        dst = tk.Yp + (row + (tk.dfer ? (size_t)(bt & 1) : 0)) * tk.cs;
     }
     const int P = tk.P;
+    const int p_hi = tk.in_ch > 0 ? tk.in_ch : P;
     const size_t rs4 = (size_t)(tk.cs >> 1);   // row stride in float4
     const float4* X4 = reinterpret_cast<const float4*>(tk.X + k);
     const float4* H4 = reinterpret_cast<const float4*>(tk.H + k);
@@ -118,13 +122,13 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
         constexpr int U = 4;   // parts whose loads are in flight together
         const int Gm = G % P;  // slot step between a group's consecutive parts
         int sl0 = (int)imod(bt - (tk.p_lo + g), P);   // slot of part p0
-        for (int p0 = tk.p_lo + g; p0 < P; p0 += U * G) {
+        for (int p0 = tk.p_lo + g; p0 < p_hi; p0 += U * G) {
             float4 xv[U], hv[U];
             int sl = sl0;
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int p = p0 + u * G;
-                if (p < P) {
+                if (p < p_hi) {
                     xv[u] = __ldcg(X4 + (size_t)sl * rs4);
                     hv[u] = __ldg(H4 + (size_t)p * rs4);
                 }
@@ -134,7 +138,7 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
             sl0 = sl;
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                if (p0 + u * G < P) acc = f4mac(acc, xv[u], hv[u]);
+                if (p0 + u * G < p_hi) acc = f4mac(acc, xv[u], hv[u]);
         }
     }
     if (G > 1) {
@@ -196,7 +200,9 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     const long long isamp = rs.io.in_sample;
     const float scale = tk.scale;
     const float2* X1 = tk.X + (size_t)imod(b - 1, P) * cs;   // block b-1 (level 0, p = 1)
-    const float2* Ypb = tk.Yp + (two ? (size_t)(b & 1) * cs : 0);
+    const float2* Ypb = tk.Yp + (two ? (size_t)(b & 1) * cs : 0);   // row 0; row q at + 2 q cs
+    const int npart = tk.k0 > 0 ? tk.k0 : 1;
+    const size_t rstride = 2 * (size_t)cs;
 
     const int nq = N >> 1;                       // window quads: samples t_end - 2N + 4q .. + 3
     const int nq_old = dfer ? nq : nq - (N0 >> 2);   // quads before this step's input
@@ -391,7 +397,11 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             const int kk = 2 * (tid + i * NT);
             if (kk < 2 * npair) {
                 if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
-                if (use_yp) ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
+                if (use_yp) {
+                    ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
+                    for (int q = 1; q < npart; ++q)
+                        ya[i] = f4add(ya[i], __ldcg(reinterpret_cast<const float4*>(Ypb + q * rstride + kk)));
+                }
             }
         }
         if (l0) gather_emit();
@@ -469,6 +479,10 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                     if (use_yp) {
                         av[u][0] = __ldcg(&Ypb[k]);
                         av[u][1] = __ldcg(&Ypb[bnk]);
+                        for (int q = 1; q < npart; ++q) {
+                            av[u][0] = cadd(av[u][0], __ldcg(&Ypb[q * rstride + k]));
+                            av[u][1] = cadd(av[u][1], __ldcg(&Ypb[q * rstride + bnk]));
+                        }
                     }
                     if (use_x1) {
                         av[u][0] = cadd(av[u][0], cmul(__ldcg(&X1[k]), __ldg(&tk.H[cs + k])));
@@ -623,6 +637,8 @@ __global__ void __launch_bounds__(C::NT) pool_kernel(Bank bank, const Task* __re
         tk.k0 = k0;
         tk.k1 = min(hi, k0 + 2 * kSpreadLanes);
         tk.p_lo = p_lo;
+        tk.in_ch = 0;    // all parts from p_lo
+        tk.out_ch = 0;   // partial-sum row 0
     }
     __syncthreads();
     spread_body<C::NT>(tk, c, dyn_smem);
@@ -688,6 +704,7 @@ static const int kNT[3] = {Cls0::NT, Cls1::NT, Cls2::NT};
 static const bool kPrefetch[3] = {Cls0::PREFETCH, Cls1::PREFETCH, Cls2::PREFETCH};
 int class_threads(int cls) { return kNT[cls]; }
 int spread_task_bins() { return 2 * kSpreadLanes; }
+int spread_task_parts() { return kSpreadParts; }
 
 size_t class_smem_bytes(int cls, int maxN) {
     size_t b = fire_smem_bytes(maxN, kPrefetch[cls]);

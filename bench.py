@@ -331,11 +331,15 @@ def run_ours(args):
     m.process_device(y, x, frames, PC_PLANAR, stream)   # fill state (steady-state FDL)
     torch.cuda.synchronize()
     prof = m.profile_kernels(prof_steps)
-    dom = max(prof, key=lambda r: r["total_ms"])
-    per_launch_s = dom["total_ms"] / 1e3 / dom["launches"]
+    dom = max(prof, key=lambda r: r["launches"])   # the level-0 kernel: one launch per base step
+    per_launch_s = dom["total_ms"] / 1e3 / dom["launches"]   # isolated launches (profile pass)
     per_launch_b = dom["alg_bytes"] / dom["launches"]
     peak, peak_kind = measured_peak_gbs()
-    achieved = per_launch_b / per_launch_s / 1e9
+    # Inside the timed region the level-0 kernel runs once per base step and
+    # consecutive launches overlap (programmatic dependent launch), so its
+    # live average duration per launch is the timed time over its launches.
+    live_launch_s = (ms / 1e3) / (frames // N0)
+    achieved = per_launch_b / live_launch_s / 1e9
     traffic = ncu_traffic().get(dom["name"])
     kernels = {r["name"]: {"launches": r["launches"], "avg_us": r["total_ms"] * 1e3 / r["launches"],
                            "share": r["total_ms"] / sum(q["total_ms"] for q in prof),
@@ -416,7 +420,10 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "alg_bytes_per_launch": per_launch_b, "avg_launch_us": per_launch_s * 1e6},
+                         "alg_bytes_per_launch": per_launch_b, "avg_launch_us": live_launch_s * 1e6,
+                         "isolated_launch_us": per_launch_s * 1e6,
+                         "how": "avg_launch_us: timed region / level-0 launches in it (one per base step, "
+                                "overlapping); isolated_launch_us: CUDA events around single launches"},
             "kernels": kernels,
             "path_alg_bytes_per_sample": bps,
             "path_roofline_frac": (bps * S * frames / (ms / 1e3)) / 1e9 / peak,

@@ -48,10 +48,7 @@ constexpr int kMacNT = 256;        // MAC CTA: 4 groups x 64 lanes, two bins per
 constexpr int kMacLanes = 64;
 constexpr int kMacBins = 2 * kMacLanes;
 constexpr int kMaxMimoLevels = 8;
-constexpr int kMaxMacTerms = 512;   // (input, part) terms one MAC task sums
-constexpr int kMacU = 4;            // terms per thread per pipeline round
-constexpr int kMacStages = 4;       // rounds of filter-spectrum loads in flight + 1
-constexpr size_t kMacSmem = sizeof(float4) * kMacStages * kMacU * kMacNT;   // 64 KB
+constexpr int kMaxMacTerms = 2048;  // (input, part) terms one MAC task sums
 
 struct MLevel {
     int N, logN, P, T, s_blocks, cs, rmask, npart;
@@ -147,22 +144,9 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 // ---------------------------------------------------------------------------
 // K2: MAC tasks (fire sums and spread partial sums)
 // ---------------------------------------------------------------------------
-// 16-byte asynchronous global -> shared copies (bypassing L1), grouped so a
-// thread can wait for all but its newest groups.
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-__global__ void __launch_bounds__(kMacNT, 3) mimo_mac_kernel(const MBank* __restrict__ bank_p,
+__global__ void __launch_bounds__(kMacNT, 4) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {
     __shared__ float4 red[(kMacNT / kMacLanes - 1) * kMacLanes];
-    extern __shared__ float4 hst[];   // filter-spectrum ring [stage][u][thread] (kMacSmem bytes)
     cudaTriggerProgrammaticLaunchCompletion();
     constexpr int G = kMacNT / kMacLanes;
     const MBank& bank = *bank_p;
@@ -209,50 +193,23 @@ __global__ void __launch_bounds__(kMacNT, 3) mimo_mac_kernel(const MBank* __rest
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
-        // Filter spectra stream from HBM through a per-thread ring of
-        // kMacStages rounds in shared memory (cp.async), so kMacStages - 1
-        // rounds of loads stay in flight while one is summed; the input
-        // spectra (L2-resident) are loaded one round ahead into registers.
-        // Each thread reads back only its own copies: no block barrier.
-        constexpr int U = kMacU, S = kMacStages;
-        const int nt = J > g ? (J - g + G - 1) / G : 0;   // terms of this group
-        const int R = (nt + U - 1) / U;                   // rounds
-        auto term = [&](int r, int u) { return g + G * (U * r + u); };
-        auto issue = [&](int r) {
-            if (r < R) {
+        // four CTAs per SM (64 registers): more warps in flight hide HBM
+        // latency better than deeper per-thread unrolling
+        constexpr int U = 4;
+        for (int j0 = g; j0 < J; j0 += U * G) {
+            float4 xv[U], hv[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int j = term(r, u);
-                    if (j < J) cp_async16(&hst[((r % S) * U + u) * kMacNT + threadIdx.x], H4 + hoff[j]);
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u * G;
+                if (j < J) {
+                    xv[u] = __ldcg(X4 + xoff[j]);
+                    hv[u] = __ldcs(H4 + hoff[j]);
                 }
             }
-            cp_async_commit();   // one group per round, empty past the end
-        };
-#pragma unroll
-        for (int r = 0; r < S - 1; ++r) issue(r);
-        float4 xa[U], xb[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int j = term(0, u);
-            if (j < J) xa[u] = __ldcg(X4 + xoff[j]);
-        }
-        for (int r = 0; r < R; ++r) {
-            issue(r + S - 1);
-            if (r + 1 < R) {
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int j = term(r + 1, u);
-                    if (j < J) xb[u] = __ldcg(X4 + xoff[j]);
-                }
-            }
-            cp_async_wait<S - 1>();   // round r has landed
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                if (term(r, u) < J) acc = f4mac(acc, xa[u], hst[((r % S) * U + u) * kMacNT + threadIdx.x]);
-#pragma unroll
-            for (int u = 0; u < U; ++u) xa[u] = xb[u];
+                if (j0 + u * G < J) acc = f4mac(acc, xv[u], hv[u]);
         }
-        cp_async_wait<0>();
     }
     if (g > 0) red[(g - 1) * kMacLanes + lane] = acc;
     __syncthreads();
@@ -454,7 +411,7 @@ cudaError_t launch_fft_stage(pcm_handle* h, int stage, int grid, const MTask* ta
 
 cudaError_t launch_mac(pcm_handle* h, int grid, const MTask* tasks, const RunState& rs, cudaStream_t st, bool pdl) {
     cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = pdl_cfg(grid, kMacNT, kMacSmem, st, attr, pdl);
+    cudaLaunchConfig_t cfg = pdl_cfg(grid, kMacNT, 0, st, attr, pdl);
     return cudaLaunchKernelEx(&cfg, mimo_mac_kernel, (const MBank*)h->d_bank, tasks, rs);
 }
 
@@ -511,7 +468,6 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
     h->maxN = Nv.back();
     h->H = std::max(1, Nv.back() / buffer_size);
     h->fft_cls = cls_of(h->maxN);
-    MCK(cudaFuncSetAttribute(mimo_mac_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMacSmem), "attr");
     if (h->fft_cls == 2) {
         MCK(cudaFuncSetAttribute(mimo_xfft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
         MCK(cudaFuncSetAttribute(mimo_yifft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");

@@ -211,6 +211,7 @@ struct pcd_plan {
     size_t njobs_max = 0;
     std::string err;
     long long launches = 0;
+    bool attrs_set = false;   // large-FFT shared memory attributes applied
 };
 
 namespace {
@@ -247,8 +248,9 @@ int run_fft_jobs(pcd_plan* p, const WS& w, int L, const std::vector<FJob>& jobs,
     DCK(cudaMemcpyAsync(d, jobs.data(), sizeof(FJob) * jobs.size(), cudaMemcpyHostToDevice, st), "job upload");
     DCK(launch_fft(p->N[L], p->logN[L], d, (int)jobs.size(), w.at<float2>(p->o_W), st), "window FFT");
     p->launches++;
-    // the job table is reused by the next call: order the host writes after this launch
-    DCK(cudaStreamSynchronize(st), "job sync");
+    // The next table upload reuses the same device buffer; it is ordered
+    // after this launch on the stream, and a copy from pageable host memory
+    // has taken the host data when cudaMemcpyAsync returns.
     return PC_OK;
 }
 
@@ -258,7 +260,6 @@ int run_ifft_jobs(pcd_plan* p, const WS& w, int L, const std::vector<IJob>& jobs
     DCK(cudaMemcpyAsync(d, jobs.data(), sizeof(IJob) * jobs.size(), cudaMemcpyHostToDevice, st), "job upload");
     DCK(launch_ifft(p->N[L], p->logN[L], d, (int)jobs.size(), w.at<float2>(p->o_W), st), "inverse FFT");
     p->launches++;
-    DCK(cudaStreamSynchronize(st), "job sync");
     return PC_OK;
 }
 
@@ -367,10 +368,10 @@ int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, voi
         DCK(cudaMemcpyAsync(w.at<float2>(p->o_W), Wh.data(), sizeof(float2) * Wh.size(), cudaMemcpyHostToDevice, st),
             "twiddles");
     }
-    for (int L = 0; L < p->M; ++L) {
+    if (!p->attrs_set) {
         DCK(cudaFuncSetAttribute(dfft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
         DCK(cudaFuncSetAttribute(difft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
-        break;
+        p->attrs_set = true;
     }
     int r = filter_spectra(p, w, d_h, st);
     if (r) return r;

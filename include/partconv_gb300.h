@@ -300,11 +300,13 @@ void pcm_destroy(pcm_handle* h);
 typedef struct pcd_plan pcd_plan;
 
 /* Layout as pc_check_layout (relaxed; P[M-1] recomputed); batch signals of
- * `length` samples; h of ir_len taps.  NULL on error (message in msg). */
+ * `length` samples; h of ir_len taps.  Builds the plan's FFT job tables on
+ * the current device (one allocation, freed by pcd_destroy); calls must run
+ * on that device.  NULL on error (message in msg). */
 pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long long length, char* msg,
                      int msglen);
-/* Device workspace the caller provides to forward/backward (no allocation
- * inside); forward leaves filter and input spectra in it for backward. */
+/* Device workspace the caller provides to forward/backward (they allocate
+ * nothing); forward leaves filter and input spectra in it for backward. */
 long long pcd_workspace_bytes(const pcd_plan* p);
 /* y[batch][length] from x[batch][length] and h[ir_len] (device pointers). */
 int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, void* d_ws, void* stream);

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,39 +43,48 @@ constexpr int kWlog = 15;
 constexpr int kMaxDLevels = 8;
 constexpr int kDhChunks = 16;   // partial sums of the dL/dh reduction (fixed order)
 
-// window FFT job: dst = rfft(w) * scale, w[n] = src[start + n] for n < 2N,
-// zero outside [0, len); half == 1 zeroes the second half ([g block, 0_N]),
-// half == 2 the first half ([0_N, h part])
-struct FJob {
-    const float* src;
-    long long len, start;
-    float2* dst;
-    float scale;
-    int half;
+// Job tables are built once per plan with addresses relative to the call's
+// buffers (DPtrs), so a call only launches kernels over tables already on
+// the device.
+enum { kSrcX = 0, kSrcH = 1, kSrcG = 2 };     // FJob sources: x, h, dL/dy
+enum { kDstY = 0, kDstGH = 1, kDstGX = 2 };   // IJob targets: y, dL/dh, dL/dx
+struct DPtrs {
+    const float* in[3];
+    float* out[3];
+    char* ws;   // workspace: spectra rows are byte offsets into it
 };
-// inverse FFT job: out = irfft(src); mode 0: dst[i] = out[i], 1: dst[i] += out[i]
-// (i < min(N, limit)); mode 2: dst[q] = out[N - q] * scale (q < min(N, limit))
-struct IJob {
-    const float2* src;
-    float* dst;
-    long long limit;
+// window FFT job: row at ws + dst_off = rfft(w) * scale, w[n] = src[start + n]
+// for n < 2N with src = in[src] + src_off, zero outside [0, len); half == 1
+// zeroes the second half ([g block, 0_N]), half == 2 the first ([0_N, h part])
+struct FJob {
+    long long src_off, len, start, dst_off;
     float scale;
-    int mode;
+    int src, half, pad;
+};
+// inverse FFT job: o = irfft(row at ws + src_off), dst = out[dst] + dst_off;
+// mode 0: dst[i] = o[i], 1: dst[i] += o[i] (i < min(N, limit)); mode 2:
+// dst[q] = o[N - q] * scale (q < min(N, limit))
+struct IJob {
+    long long src_off, dst_off, limit;
+    float scale;
+    int dst, mode, pad;
 };
 
 template <int NT, int MAXB>
-__global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs, int N, int logN, const float2* W,
-                                                  int wlog) {
+__global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs, DPtrs ptr, int N, int logN,
+                                                  const float2* W, int wlog) {
     extern __shared__ float4 dyn_smem[];
     float2* s = reinterpret_cast<float2*>(dyn_smem);
     float2* twt = s + N;
     const FJob jb = jobs[blockIdx.x];
+    const float* src = ptr.in[jb.src] + jb.src_off;
+    float2* dst = reinterpret_cast<float2*>(ptr.ws + jb.dst_off);
     const int lo = jb.half == 2 ? N : 0, hi = jb.half == 1 ? N : 2 * N;   // live window samples [lo, hi)
     for (int n = threadIdx.x; n < N; n += NT) {
         const long long i = jb.start + 2LL * n;
         float a = 0.f, b = 0.f;
-        if (2 * n >= lo && 2 * n < hi && i >= 0 && i < jb.len) a = jb.src[i];
-        if (2 * n + 1 >= lo && 2 * n + 1 < hi && i + 1 >= 0 && i + 1 < jb.len) b = jb.src[i + 1];
+        if (2 * n >= lo && 2 * n < hi && i >= 0 && i < jb.len) a = src[i];
+        if (2 * n + 1 >= lo && 2 * n + 1 < hi && i + 1 >= 0 && i + 1 < jb.len) b = src[i + 1];
         s[n] = make_float2(a, b);
     }
     load_twiddles<NT>(twt, logN, W, wlog);
@@ -85,24 +95,26 @@ __global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs,
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
         rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
-        jb.dst[k] = make_float2(xk.x * jb.scale, xk.y * jb.scale);
-        if (N - k != k) jb.dst[N - k] = make_float2(xnk.x * jb.scale, xnk.y * jb.scale);
+        dst[k] = make_float2(xk.x * jb.scale, xk.y * jb.scale);
+        if (N - k != k) dst[N - k] = make_float2(xnk.x * jb.scale, xnk.y * jb.scale);
     }
 }
 
 template <int NT, int MAXB>
-__global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs, int N, int logN, const float2* W,
-                                                   int wlog) {
+__global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs, DPtrs ptr, int N, int logN,
+                                                   const float2* W, int wlog) {
     extern __shared__ float4 dyn_smem[];
     float2* s = reinterpret_cast<float2*>(dyn_smem);
     float2* twt = s + N;
     const IJob jb = jobs[blockIdx.x];
+    const float2* src = reinterpret_cast<const float2*>(ptr.ws + jb.src_off);
+    float* dst = ptr.out[jb.dst] + jb.dst_off;
     load_twiddles<NT>(twt, logN, W, wlog);
     __syncthreads();
     const Twiddles tw{twt, logN};
     for (int k = threadIdx.x; k <= N / 2; k += NT) {
         float2 zk, znk;
-        irfft_merge(jb.src[k], jb.src[N - k], k, logN, tw, zk, znk);
+        irfft_merge(src[k], src[N - k], k, logN, tw, zk, znk);
         s[k] = zk;
         if (k != 0 && k != N / 2) s[N - k] = znk;
     }
@@ -111,9 +123,9 @@ __global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs
     const float* sf = reinterpret_cast<const float*>(s);
     const int n = jb.limit < N ? (int)jb.limit : N;
     for (int i = threadIdx.x; i < n; i += NT) {
-        if (jb.mode == 0) jb.dst[i] = sf[i];
-        else if (jb.mode == 1) jb.dst[i] += sf[i];
-        else jb.dst[i] = sf[N - i] * jb.scale;
+        if (jb.mode == 0) dst[i] = sf[i];
+        else if (jb.mode == 1) dst[i] += sf[i];
+        else dst[i] = sf[N - i] * jb.scale;
     }
 }
 
@@ -176,24 +188,26 @@ __global__ void ddh_reduce_kernel(const float2* __restrict__ Dpart, float2* __re
 
 int cls_of(int N) { return N <= 1024 ? 0 : (N <= 4096 ? 1 : 2); }
 
-cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const float2* W, cudaStream_t st) {
+cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const DPtrs& ptr, const float2* W,
+                       cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
     const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
-        case 0: dfft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, N, logN, W, kWlog); break;
-        case 1: dfft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
-        default: dfft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
+        case 0: dfft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
+        case 1: dfft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
+        default: dfft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_ifft(int N, int logN, const IJob* jobs, int njobs, const float2* W, cudaStream_t st) {
+cudaError_t launch_ifft(int N, int logN, const IJob* jobs, int njobs, const DPtrs& ptr, const float2* W,
+                        cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
     const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
-        case 0: difft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, N, logN, W, kWlog); break;
-        case 1: difft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
-        default: difft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, N, logN, W, kWlog); break;
+        case 0: difft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
+        case 1: difft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
+        default: difft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
     }
     return cudaGetLastError();
 }
@@ -206,12 +220,30 @@ struct pcd_plan {
     std::vector<int> N, P, logN, cs, nb, nbg;
     std::vector<long long> s;
     // workspace offsets (bytes)
-    size_t o_W = 0, o_jobs = 0, o_ijobs = 0, total = 0;
+    size_t o_W = 0, total = 0;
     std::vector<size_t> o_H, o_X, o_Y, o_Dp, o_D;
-    size_t njobs_max = 0;
+    // job tables (device, built at creation): per level and kind, byte offset
+    // into d_tab and job count
+    struct Tab {
+        size_t off = 0;
+        int n = 0;
+    };
+    enum Kind { kFH, kFX, kIY, kFGP, kIGH, kFGX, kIGX, kKinds };
+    std::vector<std::array<Tab, kKinds>> tab;
+    char* d_tab = nullptr;
+    int device = -1;
     std::string err;
     long long launches = 0;
     bool attrs_set = false;   // large-FFT shared memory attributes applied
+    ~pcd_plan() {
+        if (d_tab) {
+            int cur = -1;
+            cudaGetDevice(&cur);
+            if (device >= 0) cudaSetDevice(device);
+            cudaFree(d_tab);
+            if (cur >= 0) cudaSetDevice(cur);
+        }
+    }
 };
 
 namespace {
@@ -241,50 +273,109 @@ struct WS {
     }
 };
 
-// upload a job table into the workspace and launch
-int run_fft_jobs(pcd_plan* p, const WS& w, int L, const std::vector<FJob>& jobs, cudaStream_t st) {
-    if (jobs.empty()) return PC_OK;
-    FJob* d = w.at<FJob>(p->o_jobs);
-    DCK(cudaMemcpyAsync(d, jobs.data(), sizeof(FJob) * jobs.size(), cudaMemcpyHostToDevice, st), "job upload");
-    DCK(launch_fft(p->N[L], p->logN[L], d, (int)jobs.size(), w.at<float2>(p->o_W), st), "window FFT");
-    p->launches++;
-    // The next table upload reuses the same device buffer; it is ordered
-    // after this launch on the stream, and a copy from pageable host memory
-    // has taken the host data when cudaMemcpyAsync returns.
-    return PC_OK;
-}
-
-int run_ifft_jobs(pcd_plan* p, const WS& w, int L, const std::vector<IJob>& jobs, cudaStream_t st) {
-    if (jobs.empty()) return PC_OK;
-    IJob* d = w.at<IJob>(p->o_ijobs);
-    DCK(cudaMemcpyAsync(d, jobs.data(), sizeof(IJob) * jobs.size(), cudaMemcpyHostToDevice, st), "job upload");
-    DCK(launch_ifft(p->N[L], p->logN[L], d, (int)jobs.size(), w.at<float2>(p->o_W), st), "inverse FFT");
+// launch the table of one kind for level L over the call's buffers
+int run_tab(pcd_plan* p, int L, int kind, const DPtrs& ptr, cudaStream_t st) {
+    const pcd_plan::Tab& t = p->tab[L][kind];
+    if (t.n <= 0) return PC_OK;
+    const float2* W = reinterpret_cast<const float2*>(ptr.ws + p->o_W);
+    const bool fwd = kind == pcd_plan::kFH || kind == pcd_plan::kFX || kind == pcd_plan::kFGP || kind == pcd_plan::kFGX;
+    if (fwd)
+        DCK(launch_fft(p->N[L], p->logN[L], reinterpret_cast<const FJob*>(p->d_tab + t.off), t.n, ptr, W, st),
+            "window FFT");
+    else
+        DCK(launch_ifft(p->N[L], p->logN[L], reinterpret_cast<const IJob*>(p->d_tab + t.off), t.n, ptr, W, st),
+            "inverse FFT");
     p->launches++;
     return PC_OK;
 }
 
-int filter_spectra(pcd_plan* p, const WS& w, const float* d_h, cudaStream_t st) {
+int filter_spectra(pcd_plan* p, const DPtrs& ptr, cudaStream_t st) {
     for (int L = 0; L < p->M; ++L) {
-        std::vector<FJob> jobs;
-        for (int q = 0; q < p->P[L]; ++q)   // row [0_N, h_q]: the window starts N before the part
-            jobs.push_back(FJob{d_h, p->ir_len, p->s[L] + (long long)q * p->N[L] - p->N[L],
-                                w.at<float2>(p->o_H[L]) + (size_t)q * p->cs[L], 1.0f / (2.0f * p->N[L]), 2});
-        int r = run_fft_jobs(p, w, L, jobs, st);
+        int r = run_tab(p, L, pcd_plan::kFH, ptr, st);
         if (r) return r;
     }
     return PC_OK;
 }
 
-int input_spectra(pcd_plan* p, const WS& w, const float* d_x, cudaStream_t st) {
+int input_spectra(pcd_plan* p, const DPtrs& ptr, cudaStream_t st) {
     for (int L = 0; L < p->M; ++L) {
-        std::vector<FJob> jobs;
-        for (int sg = 0; sg < p->B; ++sg)
-            for (int b = 0; b < p->nb[L]; ++b)
-                jobs.push_back(FJob{d_x + (size_t)sg * p->T, p->T, (long long)(b - 1) * p->N[L] - p->s[L],
-                                    w.at<float2>(p->o_X[L]) + ((size_t)sg * p->nb[L] + b) * p->cs[L], 1.0f, 0});
-        int r = run_fft_jobs(p, w, L, jobs, st);
+        int r = run_tab(p, L, pcd_plan::kFX, ptr, st);
         if (r) return r;
     }
+    return PC_OK;
+}
+
+// every job table of the plan, relative to the call's buffers (see DPtrs)
+int build_tables(pcd_plan* p) {
+    std::vector<char> host;
+    auto add = [&](auto&& jobs) -> pcd_plan::Tab {
+        pcd_plan::Tab t;
+        t.off = host.size();
+        t.n = (int)jobs.size();
+        const size_t bytes = sizeof(jobs[0]) * jobs.size();
+        host.resize(host.size() + ((bytes + 255) & ~(size_t)255));
+        if (bytes) std::memcpy(host.data() + t.off, jobs.data(), bytes);
+        return t;
+    };
+    const long long T = p->T;
+    p->tab.assign(p->M, {});
+    for (int L = 0; L < p->M; ++L) {
+        const int N = p->N[L], P = p->P[L], nb = p->nb[L], nbg = p->nbg[L];
+        const long long row = (long long)sizeof(float2) * p->cs[L];
+        const long long sL = p->s[L];
+        auto& tb = p->tab[L];
+        std::vector<FJob> f;
+        std::vector<IJob> v;
+        for (int q = 0; q < P; ++q)   // H_q = rfft([0_N, h part q]) / 2N: the window starts N before the part
+            f.push_back(FJob{0, p->ir_len, sL + (long long)q * N - N, (long long)p->o_H[L] + q * row,
+                             1.0f / (2.0f * N), kSrcH, 2, 0});
+        tb[pcd_plan::kFH] = add(f);
+        f.clear();
+        for (int sg = 0; sg < p->B; ++sg)   // X_b = rfft(x[(b-1)N - s_L, (b+1)N - s_L))
+            for (int b = 0; b < nb; ++b)
+                f.push_back(FJob{sg * T, T, (long long)(b - 1) * N - sL,
+                                 (long long)p->o_X[L] + ((long long)sg * nb + b) * row, 1.0f, kSrcX, 0, 0});
+        tb[pcd_plan::kFX] = add(f);
+        f.clear();
+        for (int sg = 0; sg < p->B; ++sg)   // y block b (level 0 stores, larger levels add)
+            for (int b = 0; b < nb; ++b) {
+                const long long t0 = (long long)b * N;
+                v.push_back(IJob{(long long)p->o_Y[L] + ((long long)sg * nb + b) * row, sg * T + t0, T - t0, 1.0f,
+                                 kDstY, L == 0 ? 0 : 1, 0});
+            }
+        tb[pcd_plan::kIY] = add(v);
+        v.clear();
+        for (int sg = 0; sg < p->B; ++sg)   // GP_b = rfft([g block b, 0_N])
+            for (int b = 0; b < nb; ++b)
+                f.push_back(FJob{sg * T, T, (long long)b * N, (long long)p->o_Y[L] + ((long long)sg * nb + b) * row,
+                                 1.0f, kSrcG, 1, 0});
+        tb[pcd_plan::kFGP] = add(f);
+        f.clear();
+        for (int q = 0; q < P; ++q) {   // dh[s_L + qN + t] = irfft(D_q)[N - t] / 2N
+            const long long t0 = sL + (long long)q * N;
+            if (t0 >= p->ir_len) break;
+            v.push_back(IJob{(long long)p->o_D[L] + q * row, t0, p->ir_len - t0, 1.0f / (2.0f * N), kDstGH, 2, 0});
+        }
+        tb[pcd_plan::kIGH] = add(v);
+        v.clear();
+        for (int sg = 0; sg < p->B; ++sg)   // G'_c = rfft(g[cN + s_L, cN + s_L + 2N)), c < nb + P - 1
+            for (int c = 0; c < nbg; ++c)
+                f.push_back(FJob{sg * T, T, (long long)c * N + sL,
+                                 (long long)p->o_Y[L] + ((long long)sg * nbg + c) * row, 1.0f, kSrcG, 0, 0});
+        tb[pcd_plan::kFGX] = add(f);
+        f.clear();
+        for (int sg = 0; sg < p->B; ++sg)   // dx block b from the adjoint sums (kept in the X rows)
+            for (int b = 0; b < nb; ++b) {
+                const long long t0 = (long long)b * N;
+                v.push_back(IJob{(long long)p->o_X[L] + ((long long)sg * nb + b) * row, sg * T + t0, T - t0, 1.0f,
+                                 kDstGX, L == 0 ? 0 : 1, 0});
+            }
+        tb[pcd_plan::kIGX] = add(v);
+        v.clear();
+    }
+    DCK(cudaGetDevice(&p->device), "cudaGetDevice");
+    DCK(cudaMalloc(&p->d_tab, std::max<size_t>(host.size(), 256)), "job table allocation");
+    DCK(cudaMemcpy(p->d_tab, host.data(), host.size(), cudaMemcpyHostToDevice), "job table upload");
     return PC_OK;
 }
 
@@ -331,7 +422,6 @@ pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long lo
         p->nbg.push_back(nb + Pv[L] - 1);   // adjoint windows reach P-1 blocks past the end
         s += (long long)Nv[L] * Pv[L];
     }
-    size_t maxjobs = 0;
     for (int L = 0; L < M; ++L) {
         const size_t cs = p->cs[L];
         p->o_H.push_back(take(off, sizeof(float2) * Pv[L] * cs));
@@ -339,13 +429,13 @@ pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long lo
         p->o_Y.push_back(take(off, sizeof(float2) * (size_t)batch * p->nbg[L] * cs));
         p->o_Dp.push_back(take(off, sizeof(float2) * (size_t)kDhChunks * Pv[L] * cs));
         p->o_D.push_back(take(off, sizeof(float2) * (size_t)Pv[L] * cs));
-        maxjobs = std::max(maxjobs, (size_t)batch * p->nbg[L]);
-        maxjobs = std::max(maxjobs, (size_t)Pv[L]);
     }
-    p->njobs_max = maxjobs;
-    p->o_jobs = take(off, sizeof(FJob) * maxjobs);
-    p->o_ijobs = take(off, sizeof(IJob) * maxjobs);
     p->total = off;
+    if (build_tables(p) != PC_OK) {
+        put(p->err.c_str());
+        delete p;
+        return nullptr;
+    }
     put("");
     return p;
 }
@@ -356,6 +446,7 @@ int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, voi
     if (!p || !d_x || !d_h || !d_y || !d_ws) return dfail(p, PC_ERR_ARG, "null pointer");
     cudaStream_t st = (cudaStream_t)stream;
     WS w{static_cast<char*>(d_ws)};
+    const DPtrs ptr{{d_x, d_h, nullptr}, {d_y, nullptr, nullptr}, w.base};
     {
         static thread_local std::vector<float2> Wh;
         if (Wh.empty()) {
@@ -373,9 +464,9 @@ int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, voi
         DCK(cudaFuncSetAttribute(difft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
         p->attrs_set = true;
     }
-    int r = filter_spectra(p, w, d_h, st);
+    int r = filter_spectra(p, ptr, st);
     if (r) return r;
-    r = input_spectra(p, w, d_x, st);
+    r = input_spectra(p, ptr, st);
     if (r) return r;
     for (int L = 0; L < p->M; ++L) {
         const int cs = p->cs[L], nb = p->nb[L];
@@ -385,14 +476,7 @@ int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, voi
             w.at<float2>(p->o_X[L]), w.at<float2>(p->o_H[L]), Y, p->B, nb, nb, p->P[L], cs, 0);
         DCK(cudaGetLastError(), "forward MAC");
         p->launches++;
-        std::vector<IJob> jobs;
-        for (int sg = 0; sg < p->B; ++sg)
-            for (int b = 0; b < nb; ++b) {
-                const long long t0 = (long long)b * p->N[L];
-                jobs.push_back(IJob{Y + ((size_t)sg * nb + b) * cs, d_y + (size_t)sg * p->T + t0, p->T - t0, 1.0f,
-                                    L == 0 ? 0 : 1});
-            }
-        r = run_ifft_jobs(p, w, L, jobs, st);
+        r = run_tab(p, L, pcd_plan::kIY, ptr, st);
         if (r) return r;
     }
     return PC_OK;
@@ -403,26 +487,22 @@ int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d
     if (!p || !d_gy || !d_ws) return dfail(p, PC_ERR_ARG, "null pointer");
     cudaStream_t st = (cudaStream_t)stream;
     WS w{static_cast<char*>(d_ws)};
+    const DPtrs ptr{{d_x, d_h, d_gy}, {nullptr, d_gh, d_gx}, w.base};
     int r;
     if (recompute) {   // rebuild what the forward pass left in the workspace
         if (!d_x || !d_h) return dfail(p, PC_ERR_ARG, "recompute needs x and h");
-        r = filter_spectra(p, w, d_h, st);
+        r = filter_spectra(p, ptr, st);
         if (r) return r;
-        r = input_spectra(p, w, d_x, st);
+        r = input_spectra(p, ptr, st);
         if (r) return r;
     }
     for (int L = 0; L < p->M; ++L) {
-        const int N = p->N[L], cs = p->cs[L], nb = p->nb[L], nbg = p->nbg[L], P = p->P[L];
+        const int cs = p->cs[L], nb = p->nb[L], nbg = p->nbg[L], P = p->P[L];
         float2* Y = w.at<float2>(p->o_Y[L]);
         // dL/dh first: it needs the input spectra X, which the adjoint pass
         // below overwrites with its own result
         if (d_gh) {
-            std::vector<FJob> fj;   // GP_b = rfft([g block b, 0_N])
-            for (int sg = 0; sg < p->B; ++sg)
-                for (int b = 0; b < nb; ++b)
-                    fj.push_back(FJob{d_gy + (size_t)sg * p->T, p->T, (long long)b * N, Y + ((size_t)sg * nb + b) * cs,
-                                      1.0f, 1});
-            r = run_fft_jobs(p, w, L, fj, st);
+            r = run_tab(p, L, pcd_plan::kFGP, ptr, st);   // GP_b = rfft([g block b, 0_N]) into Y
             if (r) return r;
             float2* Dp = w.at<float2>(p->o_Dp[L]);
             float2* D = w.at<float2>(p->o_D[L]);
@@ -432,22 +512,11 @@ int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d
             ddh_reduce_kernel<<<(P * cs + 255) / 256, 256, 0, st>>>(Dp, D, P, cs, kDhChunks);
             DCK(cudaGetLastError(), "dL/dh reduction");
             p->launches += 2;
-            std::vector<IJob> ij;   // dh[s_L + qN + t] = irfft(D_q)[N - t] / 2N
-            for (int q = 0; q < P; ++q) {
-                const long long t0 = p->s[L] + (long long)q * N;
-                if (t0 >= p->ir_len) break;
-                ij.push_back(IJob{D + (size_t)q * cs, d_gh + t0, p->ir_len - t0, 1.0f / (2.0f * N), 2});
-            }
-            r = run_ifft_jobs(p, w, L, ij, st);
+            r = run_tab(p, L, pcd_plan::kIGH, ptr, st);   // dh[s_L + qN + t] = irfft(D_q)[N - t] / 2N
             if (r) return r;
         }
         if (d_gx) {
-            std::vector<FJob> fj;   // G'_c = rfft(g[cN + s_L, cN + s_L + 2N)), c < nb + P - 1
-            for (int sg = 0; sg < p->B; ++sg)
-                for (int c = 0; c < nbg; ++c)
-                    fj.push_back(FJob{d_gy + (size_t)sg * p->T, p->T, (long long)c * N + p->s[L],
-                                      Y + ((size_t)sg * nbg + c) * cs, 1.0f, 0});
-            r = run_fft_jobs(p, w, L, fj, st);
+            r = run_tab(p, L, pcd_plan::kFGX, ptr, st);   // G'_c into Y
             if (r) return r;
             float2* Z = w.at<float2>(p->o_X[L]);   // adjoint sums replace the input spectra
             const long long total = (long long)p->B * nb * cs;
@@ -455,14 +524,7 @@ int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d
                 Y, w.at<float2>(p->o_H[L]), Z, p->B, nbg, nb, P, cs, 1);
             DCK(cudaGetLastError(), "adjoint MAC");
             p->launches++;
-            std::vector<IJob> ij;
-            for (int sg = 0; sg < p->B; ++sg)
-                for (int b = 0; b < nb; ++b) {
-                    const long long t0 = (long long)b * N;
-                    ij.push_back(IJob{Z + ((size_t)sg * nb + b) * cs, d_gx + (size_t)sg * p->T + t0, p->T - t0, 1.0f,
-                                      L == 0 ? 0 : 1});
-                }
-            r = run_ifft_jobs(p, w, L, ij, st);
+            r = run_tab(p, L, pcd_plan::kIGX, ptr, st);
             if (r) return r;
         }
     }

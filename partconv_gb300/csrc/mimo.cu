@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 // ---------------------------------------------------------------------------
 // K2: MAC tasks (fire sums and spread partial sums)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMacNT, 3) mimo_mac_kernel(const MBank* __restrict__ bank_p,
+__global__ void __launch_bounds__(kMacNT, 4) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {
     __shared__ float4 red[(kMacNT / kMacLanes - 1) * kMacLanes];
     cudaTriggerProgrammaticLaunchCompletion();
@@ -193,32 +193,22 @@ __global__ void __launch_bounds__(kMacNT, 3) mimo_mac_kernel(const MBank* __rest
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
-        // Software-pipelined: round r + 1's loads are issued before round r
-        // is summed, so a thread always has one round of filter-spectrum
-        // (HBM) and input-spectrum (L2) loads in flight.
+        // four CTAs per SM (64 registers): more warps in flight hide HBM
+        // latency better than deeper per-thread unrolling
         constexpr int U = 4;
-        float4 xv[U], hv[U], xn[U], hn[U];
-        auto load = [&](int j0, float4* xr, float4* hr) {
+        for (int j0 = g; j0 < J; j0 += U * G) {
+            float4 xv[U], hv[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u * G;
                 if (j < J) {
-                    xr[u] = __ldcg(X4 + xoff[j]);
-                    hr[u] = __ldcs(H4 + hoff[j]);
+                    xv[u] = __ldcg(X4 + xoff[j]);
+                    hv[u] = __ldcs(H4 + hoff[j]);
                 }
             }
-        };
-        load(g, xv, hv);
-        for (int j0 = g; j0 < J; j0 += U * G) {
-            if (j0 + U * G < J) load(j0 + U * G, xn, hn);
 #pragma unroll
             for (int u = 0; u < U; ++u)
                 if (j0 + u * G < J) acc = f4mac(acc, xv[u], hv[u]);
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                xv[u] = xn[u];
-                hv[u] = hn[u];
-            }
         }
     }
     if (g > 0) red[(g - 1) * kMacLanes + lane] = acc;

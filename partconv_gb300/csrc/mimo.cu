@@ -44,7 +44,7 @@ using namespace pcg;
 namespace {
 
 constexpr int kWlog = 15;
-constexpr int kMacNT = 256;        // MAC CTA: 4 groups x 64 lanes, two bins per lane
+constexpr int kMacNT = 128;        // MAC CTA: 2 groups x 64 lanes, two bins per lane
 constexpr int kMacLanes = 64;
 constexpr int kMacBins = 2 * kMacLanes;
 constexpr int kMaxMimoLevels = 8;
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 // ---------------------------------------------------------------------------
 // K2: MAC tasks (fire sums and spread partial sums)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMacNT, 4) mimo_mac_kernel(const MBank* __restrict__ bank_p,
+__global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {
     __shared__ float4 red[(kMacNT / kMacLanes - 1) * kMacLanes];
     cudaTriggerProgrammaticLaunchCompletion();
@@ -193,8 +193,8 @@ __global__ void __launch_bounds__(kMacNT, 4) mimo_mac_kernel(const MBank* __rest
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
-        // four CTAs per SM (64 registers): more warps in flight hide HBM
-        // latency better than deeper per-thread unrolling
+        // eight 128-thread CTAs per SM (64 registers): more, smaller CTAs in
+        // flight hide HBM latency better than deeper per-thread unrolling
         constexpr int U = 4;
         for (int j0 = g; j0 < J; j0 += U * G) {
             float4 xv[U], hv[U];

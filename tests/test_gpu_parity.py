@@ -41,6 +41,10 @@ LAYOUTS = [
     ([128, 1024], [40, 0], 12000),                # slack 32 steps, window capped at T - 2 = 6
     ([64, 512], [9, 0], 6000),                    # window of one step
     ([256, 2048, 16384], [14, 14, 0], 131072),    # config-1 IR length, strict chain
+    # many parts: spread tasks split into several partial-sum rows
+    ([64, 512], [40, 0], 12000),                  # level 0: 38 parts beyond the first two (3 rows)
+    ([64, 512], [8, 0], 64 * 8 + 512 * 40),       # in-step level 1 with 40 parts (3 rows)
+    ([32], [0], 3200),                            # one level, 100 parts (7 rows)
 ]
 DEFERRED = LAYOUTS[7:]
 

@@ -45,6 +45,7 @@ LAYOUTS = [
     ([64, 512], [40, 0], 12000),                  # level 0: 38 parts beyond the first two (3 rows)
     ([64, 512], [8, 0], 64 * 8 + 512 * 40),       # in-step level 1 with 40 parts (3 rows)
     ([32], [0], 3200),                            # one level, 100 parts (7 rows)
+    ([2048, 16384], [8, 0], 60000),               # base block in the 4096 class (no prefetch path)
 ]
 DEFERRED = LAYOUTS[7:]
 

@@ -185,7 +185,6 @@ struct pc_handle {
 
     long long frame_num = 0;
     long long launches = 0;
-    bool direct_prev_l0 = false;   // the last direct launch was a level-0-class kernel
 };
 
 namespace {
@@ -233,22 +232,17 @@ int phase_of(const pc_handle* h, long long step) { return (int)(step & (long lon
 
 // One base step by direct launches (classes with work in this phase).
 // first: the preceding work in the stream is not one of this handle's step
-// kernels, so the launch must not overlap it.  A level-0-class kernel
-// overlaps only the previous step's level-0-class kernel: its larger levels'
-// spread tasks start before its dependency wait and must not overlap a fire
-// of another class.
+// kernels, so the launch must not overlap it.
 int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool first) {
     const int ph = phase_of(h, rs.step_base);
     for (int k = 0; k < kClasses; ++k) {
         const int cls = (h->l0_class + k) % kClasses;   // level-0 class first
         const int n = h->cnt[cls][ph];
         if (n <= 0) continue;
-        const bool pdl = !first && (cls != h->l0_class || h->direct_prev_l0);
         CK(launch_step_class(cls, n, h->class_maxN[cls], h->bank, h->d_tasks + h->off[cls][ph], rs, nullptr, 0, st,
-                             pdl),
+                             !first),
            "step launch");
         first = false;
-        h->direct_prev_l0 = (cls == h->l0_class);
         h->launches += 1;
     }
     // deferred fires of blocks completed by this step, in stream order (a
@@ -259,7 +253,6 @@ int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool f
                              !first),
            "deferred fire launch");
         first = false;
-        h->direct_prev_l0 = false;
         h->launches += 1;
     }
     return PC_OK;
@@ -614,9 +607,6 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                     t.out_ch = r;
                     t.lv_index = li;
                     t.dfer = dwin[li] > 0;
-                    // early: its level's fires never run in this kernel class
-                    // within a step (deferred, or another class)
-                    t.mix_mode = (l.T > 1 && (dwin[li] > 0 || fire_class_of(l.N) != sc)) ? 1 : 0;
                     lists[sc][g].push_back(t);
                 }
             h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0 * l.npart) * (hi - lo);

@@ -58,8 +58,7 @@ struct DevPC {
 // inverse FFT, output (level 0 also emits the step's output); k0 holds the
 // number of partial-sum rows to add (0 means 1).  kind 1 (spread): partial
 // FDL MAC over bins [k0, k1) and parts [p_lo, in_ch) (in_ch 0: up to P) of
-// a level's next block, written to partial-sum row out_ch; mix_mode 1 lets
-// it start before the kernel's grid dependency wait.
+// a level's next block, written to partial-sum row out_ch.
 struct Task {
     int kind, N, logN, P;
     int T, s_blocks, cs, rmask;

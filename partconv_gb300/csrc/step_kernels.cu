@@ -577,14 +577,7 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     __syncthreads();
     const long long c = rs.step_base + step_in_batch;
     if (tk.kind == 1) {
-        // A spread marked early (mix_mode 1: a larger level whose fires run
-        // outside this kernel class or are deferred) reads only spectra of
-        // fires that completed before this launch and writes rows no running
-        // kernel reads; the fires involved are ordered by full graph edges
-        // (direct launches overlap a level-0-class kernel only with the
-        // previous step's).  It runs at once, beside the previous step's
-        // tail.  Other spreads read the previous step's spectra and wait.
-        if (tk.mix_mode != 1) cudaGridDependencySynchronize();
+        cudaGridDependencySynchronize();
         spread_body<C::NT>(tk, c, dyn_smem);
         return;
     }

@@ -26,13 +26,13 @@ _lock = threading.Lock()
 
 
 def candidate_layouts(ir_len: int, N0: int, max_block: int = 16384):
-    """Level chains with ratios 2, 4 and 8 and largest blocks up to
+    """Level chains with ratios 2, 4, 8 and 16 and largest blocks up to
     max_block, each with minimum slack (every level fires within its step)
     and with the reference's strict slack (larger levels' fires run beside
     later steps), plus the one-level uniform layout for short IRs."""
     seen, out = set(), []
     for strict in (False, True):
-        for ratio in (2, 4, 8):
+        for ratio in (2, 4, 8, 16):
             mb = N0
             while mb * ratio <= max_block:
                 mb *= ratio

@@ -635,10 +635,12 @@ def run_plain_mono(args):
         m.run(out, x[b * N0:(b + 1) * N0], N0)
         lat[b] = time.perf_counter() - t0
     plain = nb * N0 / FS / float(lat.sum())
-    # the CPU oracle on one core over the same signal, and parity
+    # the CPU restatement over the same signal: one core, and reference-shaped
+    # (one worker thread per level, as the reference's level threads)
     t0 = time.perf_counter()
     ref = oracle.OracleMulti(N0, 1, 1, pcs).run(x)[:, 0]
     cpu_s = time.perf_counter() - t0
+    _, lvl_s = oracle.run_leveled(c["N"], c["P"], c["h"], x[:, 0])
     ref64 = wl.conv_fp64(c["x"], c["h"])
     n = len(ref64)
     line = {"metric": "audio-s/s (plain mono drop-in, cfg1)", "value": proc, "unit": "audio-s/s", "n_gpus": 1,
@@ -653,8 +655,10 @@ def run_plain_mono(args):
                                             "p99": float(np.percentile(lat, 99) * 1e6),
                                             "max": float(lat.max() * 1e6)},
                              "deadline_us": N0 / FS * 1e6},
-            "cpu_baseline": {"value": audio_s / cpu_s, "unit": "audio-s/s", "cores": 1, "kind": "port",
-                             "sample": "whole signal; restated CPU path (own FFT); reference FFTW build unavailable"},
+            "cpu_baseline": {"value": audio_s / lvl_s, "unit": "audio-s/s", "cores": len(c["N"]), "kind": "port",
+                             "sample": "whole signal, one worker thread per level (reference-shaped); restated "
+                                       "CPU path (own FFT); reference FFTW build unavailable"},
+            "cpu_single_core": {"value": audio_s / cpu_s, "unit": "audio-s/s", "cores": 1},
             "parity": {"rel_l2_vs_oracle": wl.rel_l2(y[:n, 0], ref[:n]), "rel_l2_vs_fp64": wl.rel_l2(y[:n, 0], ref64),
                        "oracle_rel_l2_vs_fp64": wl.rel_l2(ref[:n], ref64), "tol": 1e-5}}
     print(json.dumps(line))

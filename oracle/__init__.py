@@ -18,4 +18,5 @@ from .oracle import (  # noqa: F401
     irfft,
     conv_direct_f64,
     run_streams,
+    run_leveled,
 )

@@ -259,3 +259,25 @@ def run_streams(layouts, irs, x_planar, buffer_size, threads=None):
     if t < 0:
         raise ValueError(msg.value.decode())
     return y, t
+
+
+def run_leveled(N, P, ir, x):
+    """One worker thread per level over a mono signal (the reference's
+    thread-per-level shape); returns (y, wall seconds).  Bit-identical to the
+    sequential minimum-latency restatement."""
+    L = lib()
+    if not hasattr(L, "_leveled"):
+        L.orc_run_leveled.argtypes = [C.c_int, _i32p, _i32p, _f32p, C.c_int, _f32p, _f32p, C.c_long, C.c_char_p,
+                                      C.c_int]
+        L.orc_run_leveled.restype = C.c_double
+        L._leveled = True
+    N = _i32(N)
+    P = _i32(P).copy()
+    ir = _f32(ir)
+    x = _f32(x).reshape(-1)
+    y = np.zeros_like(x)
+    msg = C.create_string_buffer(256)
+    t = L.orc_run_leveled(len(N), _ip(N), _ip(P), _fp(ir), len(ir), _fp(x), _fp(y), len(x), msg, 256)
+    if t < 0:
+        raise ValueError(msg.value.decode())
+    return y, t

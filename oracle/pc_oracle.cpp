@@ -489,6 +489,7 @@ struct Filter : Convolver {
 struct MinLatFilter : Convolver {
     std::vector<long> s;
     std::vector<int> T, R;
+    int only = -1;   // >= 0: run and emit that level alone (one worker per level)
     std::vector<RealFFT> fft;
     std::vector<std::vector<float>> H, X, Y, yring;
     std::vector<float> xring, win, blk, prev_out;
@@ -552,12 +553,17 @@ struct MinLatFilter : Convolver {
         const long t = c * (long)N0;
         for (int i = 0; i < N0; ++i) xring[(size_t)((t + i) & (Rin - 1))] = in[i];
         for (int L = 0; L < M; ++L) {
+            if (only >= 0 && L != only) continue;
             long q = c + 1 + s[L] / N0;
             if (q % T[L] == 0) run_block(L, q / T[L] - 1);
         }
-        for (int i = 0; i < N0; ++i) out[i] = yring[0][(size_t)((t + i) & (R[0] - 1))];
-        for (int L = 1; L < M; ++L)
-            for (int i = 0; i < N0; ++i) out[i] += yring[L][(size_t)((t + i) & (R[L] - 1))];
+        if (only >= 0) {
+            for (int i = 0; i < N0; ++i) out[i] = yring[only][(size_t)((t + i) & (R[only] - 1))];
+        } else {
+            for (int i = 0; i < N0; ++i) out[i] = yring[0][(size_t)((t + i) & (R[0] - 1))];
+            for (int L = 1; L < M; ++L)
+                for (int i = 0; i < N0; ++i) out[i] += yring[L][(size_t)((t + i) & (R[L] - 1))];
+        }
         ++c;
     }
     void process(const float* in, float* out) override { step(in, out); }
@@ -813,6 +819,44 @@ double orc_run_streams(int S, const int* M, const int* N_flat, const int* P_flat
     std::vector<std::thread> th;
     for (int t = 0; t < threads; ++t) th.emplace_back(work);
     for (auto& t : th) t.join();
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Reference-shaped CPU throughput: one worker thread per level, as the
+// reference runs each level on its own thread (src/partconvMulti.cpp:473-694).
+// Each worker convolves the whole signal with its level's part of the IR;
+// the level outputs are then summed in level order, the order of the
+// sequential restatement, so the result is bit-identical to it.  Returns
+// wall seconds (-1 on a bad layout).
+double orc_run_leveled(int M, const int* N, const int* P, const float* ir, int ir_len, const float* in,
+                       float* out, long frames, char* msg, int msglen) {
+    std::vector<std::unique_ptr<MinLatFilter>> f(M);
+    for (int L = 0; L < M; ++L) {
+        f[L].reset(new MinLatFilter());
+        std::vector<int> Pt(P, P + M);
+        std::string err;
+        if (f[L]->setup(M, N, Pt.data(), ir, ir_len, err)) {
+            put_msg(msg, msglen, err);
+            return -1.0;
+        }
+        f[L]->only = L;
+    }
+    const int N0 = N[0];
+    const long nb = frames / N0;
+    std::vector<std::vector<float>> y(M, std::vector<float>((size_t)nb * N0));
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> th;
+    for (int L = 0; L < M; ++L)
+        th.emplace_back([&, L]() {
+            for (long b = 0; b < nb; ++b) f[L]->step(in + b * N0, y[L].data() + b * N0);
+        });
+    for (auto& t : th) t.join();
+    for (long i = 0; i < nb * N0; ++i) {
+        float v = y[0][i];
+        for (int L = 1; L < M; ++L) v += y[L][i];
+        out[i] = v;
+    }
     auto t1 = std::chrono::steady_clock::now();
     return std::chrono::duration<double>(t1 - t0).count();
 }

@@ -229,3 +229,17 @@ def test_run_streams_matches_multi():
     assert t >= 0
     for s in range(3):
         assert rel_l2(y[s], conv_fp64(x[s], irs[s], x.shape[1])) < 1e-6
+
+
+def test_leveled_workers_equal_sequential_restatement():
+    """The reference-shaped CPU baseline (one worker thread per level, level
+    outputs summed in level order) gives the sequential restatement's bits."""
+    from partconv_gb300 import workloads as wl
+
+    rng = np.random.default_rng(3)
+    for N, P, L in [([64, 256, 1024], [4, 3, 0], 9000), ([128, 1024, 8192], [14, 14, 0], 40000), ([32], [0], 500)]:
+        h = wl.decaying_ir(rng, L, 0.3)
+        x = (0.1 * rng.standard_normal(N[0] * 200)).astype(np.float32)
+        y1, t = oracle.run_leveled(N, P, h, x)
+        yr, _ = oracle.run_streams([(N, P)], [h], x[None, :], N[0])
+        assert np.array_equal(y1, yr[0]) and t > 0

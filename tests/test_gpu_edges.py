@@ -59,7 +59,7 @@ def test_ir_shorter_than_a_block(gpu, L):
 
 def test_linearity(gpu):
     rng = np.random.default_rng(4)
-    h = wl.decaying_ir(rng, 30000, 0.4)
+    h = wl.decaying_ir(rng, 40000, 0.4)
     pcs = [dict(ir=h, N=[256, 2048, 16384], P=[14, 14, 0])]
     n = 256 * 400
     x1 = (0.1 * rng.standard_normal(n)).astype(np.float32)

@@ -109,29 +109,67 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
     const float* in = rs.io.in + (c - rs.io.step0) * rs.io.in_step + (long long)t.ch * rs.io.in_ch;
     float* xr = xring + (size_t)t.ch * (rin_mask + 1);
     load_twiddles<NT>(twt, logN, bank.W, bank.wlog);
+    const long long isamp = rs.io.in_sample;
+    const long long b = block_of(l, c);
+    float2* Xs = l.X + ((size_t)t.ch * l.P + (size_t)imod(b, l.P)) * l.cs;
+    // A window that lies wholly in this call's input is transformed before
+    // the dependency wait (it reads only the input), its spectrum held in
+    // registers until after the wait, when the spectrum ring may be written.
+    constexpr int KMAX = 2 * MAXB + 1;   // bin pairs per thread (N <= 4 NT MAXB)
+    const bool early = MAXB <= 2 && (c - rs.io.step0) * N0 >= 2LL * N - N0;
+    float2 xk_r[MAXB <= 2 ? KMAX : 1][2];
+    if constexpr (MAXB <= 2) {
+        if (early) {
+            for (int n = tid; n < N; n += NT) {
+                const long long j = t_end - 2LL * N + 2LL * n - t_new;   // may be negative: earlier blocks
+                s[n] = make_float2(in[j * isamp], in[(j + 1) * isamp]);
+            }
+            __syncthreads();
+            const Twiddles tw{twt, logN};
+            fft_smem<NT, MAXB>(s, N, logN, tw, false);
+#pragma unroll
+            for (int q = 0; q < KMAX; ++q) {
+                const int k = tid + q * NT;
+                if (k <= N / 2) rfft_split(s[k], s[k == 0 ? 0 : N - k], k, logN, tw, xk_r[q][0], xk_r[q][1]);
+            }
+        }
+    }
     cudaGridDependencySynchronize();
+    if constexpr (MAXB <= 2) {
+        if (early) {
+#pragma unroll
+            for (int q = 0; q < KMAX; ++q) {
+                const int k = tid + q * NT;
+                if (k <= N / 2) {
+                    Xs[k] = xk_r[q][0];
+                    if (N - k != k) Xs[N - k] = xk_r[q][1];
+                }
+            }
+            if (t.level == 0)   // the ring keeps the input history for later calls
+                for (int i = tid; i < N0; i += NT) xr[(t_new + i) & rin_mask] = in[i * isamp];
+            return;
+        }
+    }
     for (int n = tid; n < N; n += NT) {
         const long long ta = t_end - 2LL * N + 2LL * n;
-        float a, b;
+        float a, bb;
         if (ta >= t_new) {
             const long long j = ta - t_new;
-            a = in[j * rs.io.in_sample];
-            b = in[(j + 1) * rs.io.in_sample];
+            a = in[j * isamp];
+            bb = in[(j + 1) * isamp];
             if (t.level == 0) {
                 xr[ta & rin_mask] = a;
-                xr[(ta + 1) & rin_mask] = b;
+                xr[(ta + 1) & rin_mask] = bb;
             }
         } else {
             a = __ldcg(&xr[ta & rin_mask]);
-            b = __ldcg(&xr[(ta + 1) & rin_mask]);
+            bb = __ldcg(&xr[(ta + 1) & rin_mask]);
         }
-        s[n] = make_float2(a, b);
+        s[n] = make_float2(a, bb);
     }
     __syncthreads();
     const Twiddles tw{twt, logN};
     fft_smem<NT, MAXB>(s, N, logN, tw, false);
-    const long long b = block_of(l, c);
-    float2* Xs = l.X + ((size_t)t.ch * l.P + (size_t)imod(b, l.P)) * l.cs;
     for (int k = tid; k <= N / 2; k += NT) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;

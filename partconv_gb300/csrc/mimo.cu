@@ -195,7 +195,6 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
     const bool active = k < t.k1;
     const int o = t.ch, P = l.P, cs = l.cs, nI = bank.nI;
     const long long c = rs.step_base;
-    cudaGridDependencySynchronize();
 
     // (input, part) iteration space
     long long bt;
@@ -227,6 +226,9 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
         hoff[j] = ((i * P + p) * cs) >> 1;
     }
     __syncthreads();
+    // the tables depend only on the task and the step: built before the
+    // wait for the input spectra of this step
+    cudaGridDependencySynchronize();
     const float4* H4 = reinterpret_cast<const float4*>(l.H + (size_t)o * nI * P * cs + k);
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -226,23 +226,16 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
         hoff[j] = ((i * P + p) * cs) >> 1;
     }
     __syncthreads();
+    // the tables depend only on the task and the step: built before the
+    // wait for the input spectra of this step
+    cudaGridDependencySynchronize();
     const float4* H4 = reinterpret_cast<const float4*>(l.H + (size_t)o * nI * P * cs + k);
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
-    // eight 128-thread CTAs per SM (64 registers): more, smaller CTAs in
-    // flight hide HBM latency better than deeper per-thread unrolling
-    constexpr int U = 4;
-    // the tables and the filter spectra depend only on the task and the
-    // step: the tables and the first round of spectrum loads go before the
-    // wait for this step's input spectra
-    float4 h_first[U];
-    if (active) {
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (g + u * G < J) h_first[u] = __ldcs(H4 + hoff[g + u * G]);
-    }
-    cudaGridDependencySynchronize();
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
+        // eight 128-thread CTAs per SM (64 registers): more, smaller CTAs in
+        // flight hide HBM latency better than deeper per-thread unrolling
+        constexpr int U = 4;
         for (int j0 = g; j0 < J; j0 += U * G) {
             float4 xv[U], hv[U];
 #pragma unroll
@@ -250,7 +243,7 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
                 const int j = j0 + u * G;
                 if (j < J) {
                     xv[u] = __ldcg(X4 + xoff[j]);
-                    hv[u] = (j0 == g) ? h_first[u] : __ldcs(H4 + hoff[j]);
+                    hv[u] = __ldcs(H4 + hoff[j]);
                 }
             }
 #pragma unroll

@@ -171,6 +171,8 @@ struct pc_handle {
     // run() staging and Relaxed carry (planar [n_out][N0])
     float* d_in1 = nullptr;
     float* d_out1 = nullptr;
+    float* h_in1 = nullptr;    // pinned host staging of one block (pc_run)
+    float* h_out1 = nullptr;
     float* d_carry = nullptr;
 
     // growable device buffers for pc_process
@@ -209,6 +211,9 @@ void free_device(pc_handle* h) {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
     if (h->arena) cudaFree(h->arena);
+    if (h->h_in1) cudaFreeHost(h->h_in1);
+    if (h->h_out1) cudaFreeHost(h->h_out1);
+    h->h_in1 = h->h_out1 = nullptr;
     h->arena = nullptr;
     if (h->d_big_in) cudaFree(h->d_big_in);
     if (h->d_big_out) cudaFree(h->d_big_out);
@@ -749,6 +754,12 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->d_rs = reinterpret_cast<RunState*>(A + off_rs);
     h->d_in1 = reinterpret_cast<float*>(A + off_in1);
     h->d_out1 = reinterpret_cast<float*>(A + off_out1);
+    // pinned staging: a callback's block crosses PCIe/C2C as a true async
+    // copy instead of a driver-staged pageable one
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&h->h_in1), sizeof(float) * (size_t)N0 * n_in, cudaHostAllocDefault),
+       "pinned staging");
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&h->h_out1), sizeof(float) * (size_t)N0 * n_out, cudaHostAllocDefault),
+       "pinned staging");
     h->d_carry = reinterpret_cast<float*>(A + so.carry);
 
     h->bank.pcs = reinterpret_cast<const DevPC*>(A + off_pcs);
@@ -1065,11 +1076,13 @@ int pc_run(pc_handle* h, float* output, const float* input, int frame_count) {
                     "frameCount (" + std::to_string(frame_count) + ") != buffer_size (" + std::to_string(h->N0) + ")");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
     const size_t in_b = sizeof(float) * (size_t)h->N0 * h->n_in, out_b = sizeof(float) * (size_t)h->N0 * h->n_out;
-    CK(cudaMemcpyAsync(h->d_in1, input, in_b, cudaMemcpyHostToDevice, h->stream), "input copy");
+    std::memcpy(h->h_in1, input, in_b);
+    CK(cudaMemcpyAsync(h->d_in1, h->h_in1, in_b, cudaMemcpyHostToDevice, h->stream), "input copy");
     int r = process_device_impl(h, h->d_out1, h->d_in1, h->N0, PC_INTERLEAVED, h->stream);
     if (r) return r;
-    CK(cudaMemcpyAsync(output, h->d_out1, out_b, cudaMemcpyDeviceToHost, h->stream), "output copy");
+    CK(cudaMemcpyAsync(h->h_out1, h->d_out1, out_b, cudaMemcpyDeviceToHost, h->stream), "output copy");
     CK(cudaStreamSynchronize(h->stream), "run sync");
+    std::memcpy(output, h->h_out1, out_b);
     return PC_OK;
 }
 

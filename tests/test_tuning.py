@@ -96,3 +96,25 @@ def test_optimal_part_on_measured_costs(gpu):
     st, _, _, msg = check_layout(N, P, 40000)
     assert st == 0, msg
     assert all(cost(n, p) > 0 for n, p in zip(N, P))
+
+
+def test_cached_layout_lookup_and_fit(tmp_path):
+    """Cache entries are keyed by GPU, base block, IR length class and batch
+    class; a lookup without a matching GPU takes the same-shape entry of
+    another, and the chosen structure is refitted to the exact length."""
+    import json
+
+    from partconv_gb300 import autotune as at
+    from partconv_gb300.multi import check_layout
+
+    path = tmp_path / "cache.json"
+    key = "Some GPU|N0=256|len=131072|batch=32"
+    path.write_text(json.dumps({key: {"best": {"N": [256, 2048, 16384], "P": [14, 14, 7], "us_per_step": 3.7},
+                                      "candidates": []}}))
+    for L in (70000, 100000, 131072):
+        N, P = at.cached_layout(L, 256, 32, cache=str(path))
+        assert N == [256, 2048, 16384] and P[:2] == [14, 14]
+        assert check_layout(N, P, L)[0] == 0
+        assert sum(n * p for n, p in zip(N, P)) >= L
+    assert at.cached_layout(5000, 256, 32, cache=str(path)) is None
+    assert at.cached_layout(100000, 128, 32, cache=str(path)) is None

@@ -177,6 +177,98 @@ __global__ void ddh_partial_kernel(const float2* __restrict__ X, const float2* _
     }
 }
 
+// Sliding forms of the two FDL sums for P <= kSlideP: a thread owns one bin
+// of one signal over a run of kSlideRun consecutive blocks and keeps the last
+// P input spectra of that bin in registers, so each block's spectrum is
+// loaded once instead of once per part.  Same sums in the same part order as
+// dmac_kernel / ddh_partial_kernel.
+constexpr int kSlideP = 16;
+constexpr int kSlideRun = 32;
+
+// Y[s][b] = sum_p X[s][b-p] H[p] (mode 0); Y[s][b] = sum_p (-1)^k conj(H[p]) X[s][b+p] (mode 1)
+__global__ void dmac_slide_kernel(const float2* __restrict__ X, const float2* __restrict__ H, float2* __restrict__ Y,
+                                  int nsig, int nxb, int nyb, int P, int cs, int mode) {
+    const int nrun = (nyb + kSlideRun - 1) / kSlideRun;
+    const long long total = (long long)nsig * nrun * cs;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % cs);
+        const long long sr = t / cs;
+        const int run = (int)(sr % nrun), sg = (int)(sr / nrun);
+        float2 h[kSlideP], w[kSlideP];   // filter bin per part; window of input spectra
+#pragma unroll
+        for (int p = 0; p < kSlideP; ++p) {
+            h[p] = make_float2(0.f, 0.f);
+            w[p] = make_float2(0.f, 0.f);
+            if (p < P) {
+                float2 v = H[(long long)p * cs + k];
+                if (mode == 1) v = (k & 1) ? make_float2(-v.x, v.y) : make_float2(v.x, -v.y);   // (-1)^k conj
+                h[p] = v;
+            }
+        }
+        const float2* Xs = X + (long long)sg * nxb * cs + k;
+        float2* Ys = Y + (long long)sg * nyb * cs + k;
+        const int b0 = run * kSlideRun, b1 = min(nyb, b0 + kSlideRun);
+        auto xat = [&](int xb) { return (xb >= 0 && xb < nxb) ? Xs[(long long)xb * cs] : make_float2(0.f, 0.f); };
+        // mode 0 walks b upwards with w[p] = X[b - p]; mode 1 walks it
+        // downwards with w[p] = X[b + p].  Each step shifts the window by one
+        // and loads the newest block into w[0].
+        const int dir = mode == 0 ? 1 : -1;
+        const int start = mode == 0 ? b0 : b1 - 1;
+#pragma unroll
+        for (int p = 0; p < kSlideP - 1; ++p)   // the window one step before `start`
+            if (p < P - 1) w[p] = xat(start - dir * (p + 1));
+        for (int i = 0, b = start; i < b1 - b0; ++i, b += dir) {
+#pragma unroll
+            for (int p = kSlideP - 1; p > 0; --p) w[p] = w[p - 1];
+            w[0] = xat(b);
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int p = 0; p < kSlideP; ++p)
+                if (p < P) acc = cadd(acc, cmul(w[p], h[p]));
+            Ys[(long long)b * cs] = acc;
+        }
+    }
+}
+
+// Dpart[s * nrun + run][p][k] = sum over blocks b of the run of
+// conj(GP[s][b][k]) X[s][b-p][k], p < P <= kSlideP (the dL/dh correlation),
+// with the last P input spectra of the bin kept in registers.
+__global__ void ddh_slide_kernel(const float2* __restrict__ X, const float2* __restrict__ GP,
+                                 float2* __restrict__ Dpart, int nsig, int nb, int P, int cs) {
+    const int nrun = (nb + kSlideRun - 1) / kSlideRun;
+    const long long total = (long long)nsig * nrun * cs;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % cs);
+        const long long sr = t / cs;
+        const int run = (int)(sr % nrun), sg = (int)(sr / nrun);
+        const float2* Xs = X + (long long)sg * nb * cs + k;
+        const float2* Gs = GP + (long long)sg * nb * cs + k;
+        const int b0 = run * kSlideRun, b1 = min(nb, b0 + kSlideRun);
+        float2 w[kSlideP], acc[kSlideP];
+#pragma unroll
+        for (int p = 0; p < kSlideP; ++p) {
+            acc[p] = make_float2(0.f, 0.f);
+            const int xb = b0 - 1 - p;   // the window one block before b0
+            w[p] = (p < P - 1 && xb >= 0) ? Xs[(long long)xb * cs] : make_float2(0.f, 0.f);
+        }
+        for (int b = b0; b < b1; ++b) {
+#pragma unroll
+            for (int p = kSlideP - 1; p > 0; --p) w[p] = w[p - 1];
+            w[0] = Xs[(long long)b * cs];
+            const float2 g = cconj(Gs[(long long)b * cs]);
+#pragma unroll
+            for (int p = 0; p < kSlideP; ++p)
+                if (p < P) acc[p] = cadd(acc[p], cmul(g, w[p]));
+        }
+        float2* D = Dpart + (sr * P) * cs + k;
+#pragma unroll
+        for (int p = 0; p < kSlideP; ++p)
+            if (p < P) D[(long long)p * cs] = acc[p];
+    }
+}
+
 __global__ void ddh_reduce_kernel(const float2* __restrict__ Dpart, float2* __restrict__ D, int P, int cs, int nchunk) {
     const int total = P * cs;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
@@ -187,6 +279,21 @@ __global__ void ddh_reduce_kernel(const float2* __restrict__ Dpart, float2* __re
 }
 
 int cls_of(int N) { return N <= 1024 ? 0 : (N <= 4096 ? 1 : 2); }
+
+// the FDL sum over parts, sliding for P <= kSlideP
+int launch_mac(const float2* X, const float2* H, float2* Y, int nsig, int nxb, int nyb, int P, int cs, int mode,
+               cudaStream_t st) {
+    if (P <= kSlideP) {
+        const long long total = (long long)nsig * ((nyb + kSlideRun - 1) / kSlideRun) * cs;
+        dmac_slide_kernel<<<(int)std::min<long long>((total + 255) / 256, 152 * 16), 256, 0, st>>>(X, H, Y, nsig, nxb,
+                                                                                                    nyb, P, cs, mode);
+    } else {
+        const long long total = (long long)nsig * nyb * cs;
+        dmac_kernel<<<(int)std::min<long long>((total + 255) / 256, 152 * 16), 256, 0, st>>>(X, H, Y, nsig, nxb, nyb,
+                                                                                              P, cs, mode);
+    }
+    return 0;
+}
 
 cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const DPtrs& ptr, const float2* W,
                        cudaStream_t st) {
@@ -427,7 +534,8 @@ pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long lo
         p->o_H.push_back(take(off, sizeof(float2) * Pv[L] * cs));
         p->o_X.push_back(take(off, sizeof(float2) * (size_t)batch * p->nb[L] * cs));
         p->o_Y.push_back(take(off, sizeof(float2) * (size_t)batch * p->nbg[L] * cs));
-        p->o_Dp.push_back(take(off, sizeof(float2) * (size_t)kDhChunks * Pv[L] * cs));
+        const size_t nrun = (size_t)(p->nb[L] + kSlideRun - 1) / kSlideRun;
+        p->o_Dp.push_back(take(off, sizeof(float2) * std::max<size_t>(kDhChunks, (size_t)batch * nrun) * Pv[L] * cs));
         p->o_D.push_back(take(off, sizeof(float2) * (size_t)Pv[L] * cs));
     }
     p->total = off;
@@ -471,9 +579,7 @@ int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, voi
     for (int L = 0; L < p->M; ++L) {
         const int cs = p->cs[L], nb = p->nb[L];
         float2* Y = w.at<float2>(p->o_Y[L]);
-        const long long total = (long long)p->B * nb * cs;
-        dmac_kernel<<<(int)std::min<long long>((total + 255) / 256, 152 * 16), 256, 0, st>>>(
-            w.at<float2>(p->o_X[L]), w.at<float2>(p->o_H[L]), Y, p->B, nb, nb, p->P[L], cs, 0);
+        r = launch_mac(w.at<float2>(p->o_X[L]), w.at<float2>(p->o_H[L]), Y, p->B, nb, nb, p->P[L], cs, 0, st);
         DCK(cudaGetLastError(), "forward MAC");
         p->launches++;
         r = run_tab(p, L, pcd_plan::kIY, ptr, st);
@@ -506,10 +612,19 @@ int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d
             if (r) return r;
             float2* Dp = w.at<float2>(p->o_Dp[L]);
             float2* D = w.at<float2>(p->o_D[L]);
-            const long long tot = (long long)kDhChunks * P * cs;
-            ddh_partial_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152 * 16), 256, 0, st>>>(
-                w.at<float2>(p->o_X[L]), Y, Dp, p->B, nb, P, cs, kDhChunks);
-            ddh_reduce_kernel<<<(P * cs + 255) / 256, 256, 0, st>>>(Dp, D, P, cs, kDhChunks);
+            int nchunk = kDhChunks;
+            if (P <= kSlideP) {
+                const int nrun = (nb + kSlideRun - 1) / kSlideRun;
+                nchunk = p->B * nrun;
+                const long long tot = (long long)nchunk * cs;
+                ddh_slide_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152 * 16), 256, 0, st>>>(
+                    w.at<float2>(p->o_X[L]), Y, Dp, p->B, nb, P, cs);
+            } else {
+                const long long tot = (long long)kDhChunks * P * cs;
+                ddh_partial_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152 * 16), 256, 0, st>>>(
+                    w.at<float2>(p->o_X[L]), Y, Dp, p->B, nb, P, cs, kDhChunks);
+            }
+            ddh_reduce_kernel<<<(P * cs + 255) / 256, 256, 0, st>>>(Dp, D, P, cs, nchunk);
             DCK(cudaGetLastError(), "dL/dh reduction");
             p->launches += 2;
             r = run_tab(p, L, pcd_plan::kIGH, ptr, st);   // dh[s_L + qN + t] = irfft(D_q)[N - t] / 2N
@@ -519,9 +634,7 @@ int pcd_backward(pcd_plan* p, const float* d_x, const float* d_h, const float* d
             r = run_tab(p, L, pcd_plan::kFGX, ptr, st);   // G'_c into Y
             if (r) return r;
             float2* Z = w.at<float2>(p->o_X[L]);   // adjoint sums replace the input spectra
-            const long long total = (long long)p->B * nb * cs;
-            dmac_kernel<<<(int)std::min<long long>((total + 255) / 256, 152 * 16), 256, 0, st>>>(
-                Y, w.at<float2>(p->o_H[L]), Z, p->B, nbg, nb, P, cs, 1);
+            launch_mac(Y, w.at<float2>(p->o_H[L]), Z, p->B, nbg, nb, P, cs, 1, st);
             DCK(cudaGetLastError(), "adjoint MAC");
             p->launches++;
             r = run_tab(p, L, pcd_plan::kIGX, ptr, st);

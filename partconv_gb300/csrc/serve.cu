@@ -111,6 +111,14 @@ struct pcs_handle {
     long long launches = 0;
     cudaEvent_t done = nullptr;
     std::vector<void*> allocs;
+    // admission scratch (IR copy and spectra jobs) still read by enqueued
+    // work: released once its event has completed, so admission never waits
+    // for the pool's stream
+    struct PendingTmp {
+        cudaEvent_t ev;
+        size_t off, bytes;
+    };
+    std::vector<PendingTmp> tmp;
 };
 
 namespace {
@@ -125,6 +133,21 @@ int sfail(pcs_handle* h, int code, const std::string& m) {
         cudaError_t e_ = (call);                                                                           \
         if (e_ != cudaSuccess) return sfail(h, PC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e_)); \
     } while (0)
+
+// return admission scratch whose work has completed (all of it when wait)
+void reap_tmp(pcs_handle* h, bool wait) {
+    for (size_t i = 0; i < h->tmp.size();) {
+        auto& t = h->tmp[i];
+        if (wait) cudaEventSynchronize(t.ev);
+        if (cudaEventQuery(t.ev) == cudaSuccess) {
+            h->fl.release(t.off, t.bytes);
+            cudaEventDestroy(t.ev);
+            h->tmp.erase(h->tmp.begin() + i);
+        } else {
+            ++i;
+        }
+    }
+}
 
 template <class T>
 cudaError_t smalloc(pcs_handle* h, T** p, size_t n) {
@@ -264,8 +287,15 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
     for (int L = 0; L < M; ++L) jobs_n += Pv[L];
     const size_t job_bytes = ((sizeof(SpectraJob) * jobs_n + kAlign - 1) & ~(kAlign - 1));
     size_t off = 0, toff = 0;
-    if (!h->fl.alloc(need, &off)) return sfail(h, PC_ERR_NOMEM, "HBM budget of the pool is exhausted");
-    if (!h->fl.alloc(ir_bytes + job_bytes, &toff)) {
+    reap_tmp(h, false);
+    auto alloc = [&](size_t bytes, size_t* o) {
+        if (h->fl.alloc(bytes, o)) return true;
+        if (h->tmp.empty()) return false;
+        reap_tmp(h, true);   // earlier admissions' scratch, once their work is done
+        return h->fl.alloc(bytes, o);
+    };
+    if (!alloc(need, &off)) return sfail(h, PC_ERR_NOMEM, "HBM budget of the pool is exhausted");
+    if (!alloc(ir_bytes + job_bytes, &toff)) {
         h->fl.release(off, need);
         return sfail(h, PC_ERR_NOMEM, "HBM budget of the pool is exhausted");
     }
@@ -370,9 +400,13 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
     SCK(cudaMemcpyAsync(h->d_slots + (size_t)id * kPoolMaxLevels, recs.data(), sizeof(Task) * M, cudaMemcpyHostToDevice,
                         h->stream),
         "descriptor upload");
-    // the spectra pass is done before the temporary space is reused
-    SCK(cudaStreamSynchronize(h->stream), "admission sync");
-    h->fl.release(toff, ir_bytes + job_bytes);
+    // the scratch returns to the pool once the spectra pass has run
+    {
+        cudaEvent_t ev;
+        SCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+        SCK(cudaEventRecord(ev, h->stream), "event record");
+        h->tmp.push_back({ev, toff, ir_bytes + job_bytes});
+    }
     pc.live = true;
     h->live++;
     *pc_id = id;
@@ -449,6 +483,8 @@ void pcs_destroy(pcs_handle* h) {
     if (!h) return;
     if (h->device >= 0) cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto& t : h->tmp) cudaEventDestroy(t.ev);
+    h->tmp.clear();
     for (void* p : h->allocs) cudaFree(p);
     for (auto d : h->d_map)
         if (d) cudaFree(d);

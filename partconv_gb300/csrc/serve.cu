@@ -111,9 +111,11 @@ struct pcs_handle {
     long long launches = 0;
     cudaEvent_t done = nullptr;
     std::vector<void*> allocs;
-    // admission scratch (IR copy and spectra jobs) still read by enqueued
-    // work: released once its event has completed, so admission never waits
-    // for the pool's stream
+    // Admission builds a PC's spectra on its own stream, so it never waits
+    // for the pool's steps; a released PC's space may still be read by
+    // enqueued steps, so it returns to the budget only once an event
+    // recorded after them has completed.
+    cudaStream_t astream = nullptr;
     struct PendingTmp {
         cudaEvent_t ev;
         size_t off, bytes;
@@ -134,7 +136,7 @@ int sfail(pcs_handle* h, int code, const std::string& m) {
         if (e_ != cudaSuccess) return sfail(h, PC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// return admission scratch whose work has completed (all of it when wait)
+// return released space whose last users have run (all of it when wait)
 void reap_tmp(pcs_handle* h, bool wait) {
     for (size_t i = 0; i < h->tmp.size();) {
         auto& t = h->tmp[i];
@@ -233,6 +235,7 @@ pcs_handle* pcs_create(int buffer_size, long long hbm_budget_bytes, int max_pcs)
     };
     if (cudaGetDevice(&h->device) != cudaSuccess) return bad();
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bad();
+    if (cudaStreamCreateWithFlags(&h->astream, cudaStreamNonBlocking) != cudaSuccess) return bad();
     if (prepare_kernels() != cudaSuccess) return bad();
     if (cudaMalloc(&h->arena, h->budget) != cudaSuccess) {
         h->arena = nullptr;
@@ -291,7 +294,7 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
     auto alloc = [&](size_t bytes, size_t* o) {
         if (h->fl.alloc(bytes, o)) return true;
         if (h->tmp.empty()) return false;
-        reap_tmp(h, true);   // earlier admissions' scratch, once their work is done
+        reap_tmp(h, true);   // space of released PCs, once the steps that used it have run
         return h->fl.alloc(bytes, o);
     };
     if (!alloc(need, &off)) return sfail(h, PC_ERR_NOMEM, "HBM budget of the pool is exhausted");
@@ -301,10 +304,12 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
     }
     char* A = h->arena + off;
     SCK(cudaSetDevice(h->device), "cudaSetDevice");
-    SCK(cudaMemsetAsync(A, 0, need, h->stream), "clear PC state");
+    // the space is free of enqueued steps (released space waits in tmp), so
+    // the admission stream may write it at once
+    SCK(cudaMemsetAsync(A, 0, need, h->astream), "clear PC state");
     float* d_ir = reinterpret_cast<float*>(h->arena + toff);
     SpectraJob* d_jobs = reinterpret_cast<SpectraJob*>(h->arena + toff + ir_bytes);
-    SCK(cudaMemcpyAsync(d_ir, ir, sizeof(float) * ir_len, cudaMemcpyHostToDevice, h->stream), "IR upload");
+    SCK(cudaMemcpyAsync(d_ir, ir, sizeof(float) * ir_len, cudaMemcpyHostToDevice, h->astream), "IR upload");
 
     PoolPC& pc = h->pcs[id];
     pc = PoolPC{};
@@ -386,9 +391,9 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
         int mN = 0;
         for (auto& j : jobs[c]) mN = std::max(mN, j.N);
         SCK(cudaMemcpyAsync(d_jobs + jo, jobs[c].data(), sizeof(SpectraJob) * jobs[c].size(), cudaMemcpyHostToDevice,
-                            h->stream),
+                            h->astream),
             "job upload");
-        SCK(launch_spectra(c, (int)jobs[c].size(), mN, d_jobs + jo, h->d_W, kWlog, h->stream), "PC spectra");
+        SCK(launch_spectra(c, (int)jobs[c].size(), mN, d_jobs + jo, h->d_W, kWlog, h->astream), "PC spectra");
         h->launches++;
         jo += jobs[c].size();
     }
@@ -397,16 +402,13 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
         h->class_maxN[fire_class_of(Nv[L])] = std::max(h->class_maxN[fire_class_of(Nv[L])], Nv[L]);
     }
     h->class_maxN[fire_class_of(h->N0)] = std::max(h->class_maxN[fire_class_of(h->N0)], h->N0);
+    // the PC's state and spectra are ready before its descriptors reach the
+    // pool's stream (waiting only for the admission work, not for steps)
+    SCK(cudaStreamSynchronize(h->astream), "admission sync");
+    h->fl.release(toff, ir_bytes + job_bytes);
     SCK(cudaMemcpyAsync(h->d_slots + (size_t)id * kPoolMaxLevels, recs.data(), sizeof(Task) * M, cudaMemcpyHostToDevice,
                         h->stream),
         "descriptor upload");
-    // the scratch returns to the pool once the spectra pass has run
-    {
-        cudaEvent_t ev;
-        SCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
-        SCK(cudaEventRecord(ev, h->stream), "event record");
-        h->tmp.push_back({ev, toff, ir_bytes + job_bytes});
-    }
     pc.live = true;
     h->live++;
     *pc_id = id;
@@ -420,8 +422,14 @@ int pcs_release(pcs_handle* h, int pc_id) {
     SCK(cudaMemcpyAsync(h->d_slots + (size_t)pc_id * kPoolMaxLevels, recs.data(), sizeof(Task) * pc.M,
                         cudaMemcpyHostToDevice, h->stream),
         "descriptor clear");
-    // stream order keeps later users of this space behind the clear above
-    h->fl.release(pc.off, pc.bytes);
+    // steps already enqueued may still use the space: it returns to the
+    // budget once they have run
+    {
+        cudaEvent_t ev;
+        SCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+        SCK(cudaEventRecord(ev, h->stream), "event record");
+        h->tmp.push_back({ev, pc.off, pc.bytes});
+    }
     pc.live = false;
     h->live--;
     return rebuild_map(h);
@@ -432,6 +440,7 @@ int pcs_release(pcs_handle* h, int pc_id) {
 // inactive PCs are copied but produce zeros.
 int pcs_step(pcs_handle* h, const float* in, float* out, int n_channels) {
     if (!h || !in || !out) return PC_ERR_ARG;
+    if (!h->tmp.empty()) reap_tmp(h, false);
     if (n_channels < 0 || n_channels > h->max_pcs) return sfail(h, PC_ERR_ARG, "bad channel count");
     SCK(cudaSetDevice(h->device), "cudaSetDevice");
     const size_t nb = sizeof(float) * (size_t)n_channels * h->N0;
@@ -490,6 +499,7 @@ void pcs_destroy(pcs_handle* h) {
         if (d) cudaFree(d);
     if (h->arena) cudaFree(h->arena);
     if (h->done) cudaEventDestroy(h->done);
+    if (h->astream) cudaStreamDestroy(h->astream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

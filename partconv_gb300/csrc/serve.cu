@@ -234,8 +234,11 @@ pcs_handle* pcs_create(int buffer_size, long long hbm_budget_bytes, int max_pcs)
         return (pcs_handle*)nullptr;
     };
     if (cudaGetDevice(&h->device) != cudaSuccess) return bad();
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bad();
-    if (cudaStreamCreateWithFlags(&h->astream, cudaStreamNonBlocking) != cudaSuccess) return bad();
+    // steps run at the device's highest priority, admission work at its lowest
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return bad();
+    if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, greatest) != cudaSuccess) return bad();
+    if (cudaStreamCreateWithPriority(&h->astream, cudaStreamNonBlocking, least) != cudaSuccess) return bad();
     if (prepare_kernels() != cudaSuccess) return bad();
     if (cudaMalloc(&h->arena, h->budget) != cudaSuccess) {
         h->arena = nullptr;

@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
             }
             __syncthreads();
             const Twiddles tw{twt, logN};
-            fft_smem_pp<NT, MAXB>(s, twt + N / 2, N, logN, tw, false);   // MAXB <= 2 here
+            fft_smem<NT, MAXB>(s, N, logN, tw, false);
 #pragma unroll
             for (int q = 0; q < KMAX; ++q) {
                 const int k = tid + q * NT;
@@ -169,8 +169,7 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
     }
     __syncthreads();
     const Twiddles tw{twt, logN};
-    if constexpr (MAXB <= 2) fft_smem_pp<NT, MAXB>(s, twt + N / 2, N, logN, tw, false);
-    else fft_smem<NT, MAXB>(s, N, logN, tw, false);
+    fft_smem<NT, MAXB>(s, N, logN, tw, false);
     for (int k = tid; k <= N / 2; k += NT) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
@@ -298,8 +297,7 @@ __global__ void __launch_bounds__(NT) mimo_yifft_kernel(const MBank* __restrict_
         if (k != 0 && k != N / 2) s[N - k] = znk;
     }
     __syncthreads();
-    if constexpr (MAXB <= 2) fft_smem_pp<NT, MAXB>(s, twt + N / 2, N, logN, tw, true);   // scratch after the table
-    else fft_smem<NT, MAXB>(s, N, logN, tw, true);
+    fft_smem<NT, MAXB>(s, N, logN, tw, true);
     const float* sf = reinterpret_cast<const float*>(s);
     const long long c = rs.step_base;
     if (t.level > 0) {
@@ -435,8 +433,7 @@ cudaError_t launch_fft_stage(pcm_handle* h, int stage, int grid, const MTask* ta
                              cudaStream_t st, bool pdl) {
     cudaLaunchAttribute attr[1];
     const int NT = h->fft_cls == 0 ? 256 : 512;
-    // N points + N/2 twiddles (+ an N-point FFT scratch up to N = 4096)
-    const size_t smem = (size_t)(h->fft_cls < 2 ? 20 : 12) * h->maxN;
+    const size_t smem = (size_t)12 * h->maxN;
     cudaLaunchConfig_t cfg = pdl_cfg(grid, NT, smem, st, attr, pdl);
     if (stage == 0) {
         switch (h->fft_cls) {
@@ -511,10 +508,6 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
     h->maxN = Nv.back();
     h->H = std::max(1, Nv.back() / buffer_size);
     h->fft_cls = cls_of(h->maxN);
-    if (h->fft_cls == 1) {
-        MCK(cudaFuncSetAttribute(mimo_xfft_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * 4096), "attr");
-        MCK(cudaFuncSetAttribute(mimo_yifft_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * 4096), "attr");
-    }
     if (h->fft_cls == 2) {
         MCK(cudaFuncSetAttribute(mimo_xfft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
         MCK(cudaFuncSetAttribute(mimo_yifft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");

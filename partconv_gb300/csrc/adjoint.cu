@@ -90,8 +90,7 @@ __global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs,
     load_twiddles<NT>(twt, logN, W, wlog);
     __syncthreads();
     const Twiddles tw{twt, logN};
-    if constexpr (MAXB <= 2) fft_smem_pp<NT, MAXB>(s, twt + N / 2, N, logN, tw, false);   // scratch after the table
-    else fft_smem<NT, MAXB>(s, N, logN, tw, false);
+    fft_smem<NT, MAXB>(s, N, logN, tw, false);
     for (int k = threadIdx.x; k <= N / 2; k += NT) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
@@ -120,8 +119,7 @@ __global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs
         if (k != 0 && k != N / 2) s[N - k] = znk;
     }
     __syncthreads();
-    if constexpr (MAXB <= 2) fft_smem_pp<NT, MAXB>(s, twt + N / 2, N, logN, tw, true);
-    else fft_smem<NT, MAXB>(s, N, logN, tw, true);
+    fft_smem<NT, MAXB>(s, N, logN, tw, true);
     const float* sf = reinterpret_cast<const float*>(s);
     const int n = jb.limit < N ? (int)jb.limit : N;
     for (int i = threadIdx.x; i < n; i += NT) {
@@ -297,14 +295,10 @@ int launch_mac(const float2* X, const float2* H, float2* Y, int nsig, int nxb, i
     return 0;
 }
 
-// shared memory: N points + N/2 twiddles, and an N-point scratch for the
-// two-buffer FFT of the classes up to N = 4096
-size_t fft_smem_bytes(int N) { return (size_t)(cls_of(N) < 2 ? 20 : 12) * N; }
-
 cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const DPtrs& ptr, const float2* W,
                        cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
-    const size_t smem = fft_smem_bytes(N);
+    const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
         case 0: dfft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
         case 1: dfft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
@@ -316,7 +310,7 @@ cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const DPtrs
 cudaError_t launch_ifft(int N, int logN, const IJob* jobs, int njobs, const DPtrs& ptr, const float2* W,
                         cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
-    const size_t smem = fft_smem_bytes(N);
+    const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
         case 0: difft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
         case 1: difft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
@@ -576,8 +570,6 @@ int pcd_forward(pcd_plan* p, const float* d_x, const float* d_h, float* d_y, voi
     if (!p->attrs_set) {
         DCK(cudaFuncSetAttribute(dfft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
         DCK(cudaFuncSetAttribute(difft_kernel<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 12 * 16384), "attr");
-        DCK(cudaFuncSetAttribute(dfft_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * 4096), "attr");
-        DCK(cudaFuncSetAttribute(difft_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * 4096), "attr");
         p->attrs_set = true;
     }
     int r = filter_spectra(p, ptr, st);

@@ -50,6 +50,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0, help="base steps for the per-kernel profile (0: 4*H)")
+    ap.add_argument("--step-blocks", type=int, default=4,
+                    help="cfg2: base blocks per step (pc_set_step_blocks); 1 = one launch per 256-sample block. "
+                         "With K > 1 the one-block figure is measured beside it")
     ap.add_argument("--layouts", default="auto", choices=["auto", "chain"],
                     help="cfg2 layouts: measured-GPU autotuner (cached) or the minimum-slack chain")
     ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"],
@@ -156,10 +159,11 @@ def ncu_traffic():
 
 
 # --------------------------------------------------------------------------
-def workload(streams: int, samples: int, layouts: str = "auto", measure: bool = True):
+def workload(streams: int, samples: int, layouts: str = "auto", measure: bool = True, align: int = 1):
     """Config 2 inputs.  layouts: "auto" = the measured-GPU autotuner's
     choice per IR length class (its cache, measuring on a miss when allowed;
-    the minimum-slack chain when not), "chain" = the minimum-slack chain."""
+    the minimum-slack chain when not), "chain" = the minimum-slack chain.
+    align: base blocks the frame count is rounded up to (zeros appended)."""
     from partconv_gb300 import autotune
     from partconv_gb300 import workloads as wl
 
@@ -174,6 +178,7 @@ def workload(streams: int, samples: int, layouts: str = "auto", measure: bool = 
     N0 = c["N0"]
     tail = max(len(h) for h in c["irs"])
     frames = samples + (tail + N0 - 1) // N0 * N0
+    frames = (frames + align * N0 - 1) // (align * N0) * (align * N0)
     x = np.zeros((streams, frames), np.float32)
     x[:, :samples] = c["x"]
     return c, x, frames
@@ -254,26 +259,31 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    c, x_host, frames = workload(args.streams, args.samples, args.layouts)
+    K = max(1, args.step_blocks)
+    c, x_host, frames = workload(args.streams, args.samples, args.layouts, align=K)
     S, N0 = x_host.shape[0], c["N0"]
+    # the workload's own length (input + IR flush); a step with K blocks pads
+    # it to a multiple of K base blocks, and only the unpadded audio counts
+    frames1 = args.samples + (max(len(h) for h in c["irs"]) + N0 - 1) // N0 * N0
     pcs = [dict(ir=h, N=N, P=P, in_ch=s, out_ch=s) for s, (h, (N, P)) in enumerate(zip(c["irs"], c["layouts"]))]
-    m = PartConvMulti()
+    m = PartConvMulti(step_blocks=K)
     m.setup_layout(FS, N0, S, S, pcs)
     info = m.info()
-    audio_s = S * frames / FS
+    K = info.step_blocks
+    audio_s = S * frames1 / FS
 
     x = torch.from_numpy(x_host).to(dev)
     y = torch.empty_like(x)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)   # 256 MB > L2
 
-    def one_step():
-        m.reset()
+    def one_step(h=m, n=frames, xd=x, yd=y):
+        h.reset()
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        m.process_device(y, x, frames, PC_PLANAR, stream)
+        h.process_device(yd, xd, n, PC_PLANAR, stream)
         e1.record(stream)
         return e0, e1
 
@@ -309,6 +319,30 @@ def run_ours(args):
     ms = max_over_ranks([np.mean([a.elapsed_time(b) for a, b in evs])], dev)[0]
     value = job_rate(ws, audio_s, ms / 1e3)
 
+    # ---- the same workload with one launch per 256-sample base block ---------------
+    one_block = None
+    if K > 1:
+        m1 = PartConvMulti()
+        m1.setup_layout(FS, N0, S, S, pcs)
+        x1 = x[:, :frames1].contiguous()
+        y1 = torch.empty_like(x1)
+        for _ in range(args.warmup):
+            one_step(m1, frames1, x1, y1)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        l1 = m1.kernel_launches()
+        ev1 = [one_step(m1, frames1, x1, y1) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        ms1 = max_over_ranks([np.mean([a.elapsed_time(b) for a, b in ev1])], dev)[0]
+        one_block = {"value": job_rate(ws, audio_s, ms1 / 1e3), "unit": "audio-s/s", "ms_per_step": ms1,
+                     "gpu_launches": int(m1.kernel_launches() - l1),
+                     "rel_l2_max_vs_step_blocks": max(
+                         float(torch.linalg.vector_norm(y1[s_] - y[s_, :frames1]) /
+                               torch.linalg.vector_norm(y1[s_]).clamp_min(1e-30)) for s_ in range(S)),
+                     "how": "same handle layout, step_blocks 1: one level-0 launch per 256-sample block"}
+        del m1, x1, y1
+
     # ---- e2e: host buffers through the C ABI (pinned), copies timed -------------
     xp = torch.from_numpy(x_host).pin_memory()
     yp = torch.empty_like(xp).pin_memory()
@@ -338,7 +372,7 @@ def run_ours(args):
     # Inside the timed region the level-0 kernel runs once per base step and
     # consecutive launches overlap (programmatic dependent launch), so its
     # live average duration per launch is the timed time over its launches.
-    live_launch_s = (ms / 1e3) / (frames // N0)
+    live_launch_s = (ms / 1e3) / (frames // (N0 * K))
     achieved = per_launch_b / live_launch_s / 1e9
     traffic = ncu_traffic().get(dom["name"])
     kernels = {r["name"]: {"launches": r["launches"], "avg_us": r["total_ms"] * 1e3 / r["launches"],
@@ -377,15 +411,16 @@ def run_ours(args):
     # ---- batched per-block latency: one base step of all streams, device time ------
     # (one block of all streams is contiguous in the interleaved layout)
     m.reset()
-    nlat = min(frames // N0, max(2 * info.hyperperiod, 256))
+    B = N0 * K   # samples of one step
+    nlat = min(frames // B, max(2 * info.hyperperiod // K, 256))
     step_ms = []
-    xi = torch.from_numpy(np.ascontiguousarray(x_host[:, : nlat * N0].T)).to(dev)
+    xi = torch.from_numpy(np.ascontiguousarray(x_host[:, : nlat * B].T)).to(dev)
     yi = torch.empty_like(xi)
     for b in range(nlat):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        m.process_device(yi[b * N0:(b + 1) * N0], xi[b * N0:(b + 1) * N0], N0, 0, stream)
+        m.process_device(yi[b * B:(b + 1) * B], xi[b * B:(b + 1) * B], B, 0, stream)
         e1.record(stream)
         step_ms.append((e0, e1))
     torch.cuda.synchronize()
@@ -405,8 +440,11 @@ def run_ours(args):
             "value": value, "unit": "audio-s/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded numpy PCG64, cfg seed 1002)",
-            "config": {"workload": f"cfg2: {S} streams x {args.samples} samples + IR flush ({frames} per stream), "
-                                   f"IR 2^14..2^19 taps, N0={N0}, one handle, graph-replayed base steps",
+            "config": {"workload": f"cfg2: {S} streams x {args.samples} samples + IR flush ({frames1} per stream), "
+                                   f"IR 2^14..2^19 taps, N0={N0}, one handle, graph-replayed steps of "
+                                   f"{K} base block{'s' if K > 1 else ''}",
+                       "step_blocks": K,
+                       "frames_processed_per_stream": frames,
                        "layouts": ("autotuned from measured GPU timings (partconv_gb300/autotune_cache.json)"
                                    if args.layouts == "auto" else "minimum-slack level chain (ratio 8, max 16384)"),
                        "layout_set": sorted({f"{N}x{P}" for N, P in c["layouts"]})[:8],
@@ -426,12 +464,15 @@ def run_ours(args):
                                 "overlapping); isolated_launch_us: CUDA events around single launches"},
             "kernels": kernels,
             "path_alg_bytes_per_sample": bps,
-            "path_roofline_frac": (bps * S * frames / (ms / 1e3)) / 1e9 / peak,
+            "path_roofline_frac": (bps * S * frames1 / (ms / 1e3)) / 1e9 / peak,
             "block_latency_us": {"p50": float(np.percentile(lat_us, 50)), "p99": float(np.percentile(lat_us, 99)),
-                                 "max": float(np.max(lat_us)), "deadline_us": N0 / FS * 1e6,
-                                 "how": "device time of one base step (all streams), single launches"},
+                                 "max": float(np.max(lat_us)), "deadline_us": B / FS * 1e6,
+                                 "how": f"device time of one step ({K} base block{'s' if K > 1 else ''}, all "
+                                        "streams), single launches"},
             "wall_s_timed_region": wall,
         }
+        if one_block:
+            line["one_block_steps"] = one_block
         if plain:
             line["plain_gpu"] = plain
             line["batched_over_plain"] = value / plain["value"]

@@ -60,6 +60,7 @@ typedef struct pc_info {
     int hyperperiod;         /* steps after which the level schedule repeats */
     long long frame_num;     /* run() calls so far (PartConvMulti::frameNum) */
     long long device_bytes;  /* device memory held by the handle */
+    int step_blocks;         /* base blocks computed per step (pc_set_step_blocks) */
 } pc_info;
 
 /*
@@ -114,6 +115,20 @@ int pc_setup_layout(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, 
  * (src/partconvMulti.cpp:1077-1111).  Call after setup; resets state.
  */
 int pc_set_relaxed(pc_handle* h, int relaxed);
+
+/*
+ * Offline throughput option, no reference counterpart: compute k base blocks
+ * per step (k a power of two, 1..8; call before setup; up to 4 are used).  Each step's
+ * level-0 work for all PCs is one launch that transforms and convolves k
+ * consecutive blocks at once, and every larger level runs beside the steps.
+ * The output equals that of k times as many one-block steps to float32
+ * rounding (the same partitions and products, summed in another order).
+ * Setup lowers k to the largest value the layouts allow (k buffer_size <=
+ * 1024, every level's N_L a multiple of k buffer_size); pc_get_info reports
+ * it.  With k > 1, pc_run returns PC_ERR_STATE and pc_process needs a
+ * multiple of k buffer_size frames.
+ */
+int pc_set_step_blocks(pc_handle* h, int k);
 
 /*
  * PartConvMulti::run(output, input, frameCount) -- src/partconvMulti.h:60,

@@ -68,8 +68,9 @@ def _len_class(ir_len: int) -> int:
     return 1 << int(np.ceil(np.log2(max(ir_len, 2))))
 
 
-def measure_layout(N, P, ir_len: int, batch: int = 32, steps: int = 0, seed: int = 0) -> float:
-    """Device time (µs) per base step of `batch` streams of this layout."""
+def measure_layout(N, P, ir_len: int, batch: int = 32, steps: int = 0, seed: int = 0, step_blocks: int = 1) -> float:
+    """Device time (µs) per base step of `batch` streams of this layout
+    (step_blocks: base blocks per launch, pc_set_step_blocks)."""
     import torch
 
     from .multi import PartConvMulti
@@ -78,9 +79,9 @@ def measure_layout(N, P, ir_len: int, batch: int = 32, steps: int = 0, seed: int
     rng = np.random.default_rng(seed)
     N0 = N[0]
     pcs = [dict(ir=wl.decaying_ir(rng, ir_len, 1.0), N=N, P=P, in_ch=s, out_ch=s) for s in range(batch)]
-    m = PartConvMulti()
+    m = PartConvMulti(step_blocks=step_blocks)
     m.setup_layout(48000, N0, batch, batch, pcs)
-    H = m.info().hyperperiod
+    H = max(m.info().hyperperiod, m.info().step_blocks)
     nsteps = steps or max(2 * H, 128)
     nsteps = (nsteps + H - 1) // H * H
     x = torch.randn(batch, nsteps * N0, device="cuda") * 0.1

@@ -147,8 +147,11 @@ struct pc_handle {
     std::vector<DevPC> h_pcs;
     std::vector<DevLevel> h_lv;
     Bank bank{};
-    int H = 1;        // hyperperiod (steps)
-    int G = 64;       // steps per captured graph (multiple of H)
+    int H = 1;        // hyperperiod (base steps)
+    int G = 64;       // base steps per captured graph (multiple of H and KB)
+    int req_kb = 1;   // base blocks per step requested (pc_set_step_blocks)
+    int KB = 1;       // base blocks per step in use: a launch computes KB level-0 blocks
+    int Hs = 1;       // task-table phases: steps (of KB base blocks) per hyperperiod
     int maxN = 0;
     int l0_class = 0;
 
@@ -157,14 +160,21 @@ struct pc_handle {
     std::vector<int> off[kClasses], cnt[kClasses];
     std::vector<double> alg_bytes[kClasses];
     // Deferred fires (levels >= 1 whose output is due more than one step
-    // after their block completes): launched after the step that completed
-    // the block, on a low-priority stream, and joined `due` steps later.
+    // after their block completes; with several base blocks per step, every
+    // level >= 1): launched after the step that completed the block, on a
+    // low-priority stream, and joined `due` steps later.
     struct DGroup {
         int cls, phase, due, off, cnt;
         double bytes;
     };
     std::vector<DGroup> dgroups;
     std::vector<std::vector<int>> dg_of_phase;   // phase -> indices into dgroups
+    // spread tasks of levels >= 1 with several base blocks per step: their own
+    // launch per step on `sside`, beside the step chain; only the levels'
+    // deferred fires wait for them
+    cudaStream_t sside = nullptr;
+    std::vector<int> sp_off, sp_cnt;
+    std::vector<double> sp_bytes;
     int class_maxN[kClasses] = {0, 0, 0};
     RunState* d_rs = nullptr;
 
@@ -228,18 +238,30 @@ void free_device(pc_handle* h) {
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
+    if (h->sside) cudaStreamDestroy(h->sside);
+    h->sside = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     h->ready = false;
 }
 
-int phase_of(const pc_handle* h, long long step) { return (int)(step & (long long)(h->H - 1)); }
+// task-table phase of the step that starts at base step `step`
+int phase_of(const pc_handle* h, long long step) { return (int)((step / h->KB) & (long long)(h->Hs - 1)); }
+
+long long floordiv(long long a, long long b) {
+    long long q = a / b;
+    return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+}
 
 // One base step by direct launches (classes with work in this phase).
 // first: the preceding work in the stream is not one of this handle's step
 // kernels, so the launch must not overlap it.
 int launch_step_direct(pc_handle* h, const RunState& rs, cudaStream_t st, bool first) {
     const int ph = phase_of(h, rs.step_base);
+    if (h->sp_cnt[ph] > 0) {   // levels' spread tasks first, in stream order
+        CK(launch_side_spreads(h->sp_cnt[ph], h->d_tasks + h->sp_off[ph], rs, nullptr, 0, st), "spread launch");
+        h->launches += 1;
+    }
     for (int k = 0; k < kClasses; ++k) {
         const int cls = (h->l0_class + k) % kClasses;   // level-0 class first
         const int n = h->cnt[cls][ph];
@@ -283,8 +305,9 @@ int build_graph(pc_handle* h) {
         cudaEvent_t done;
     };
     std::vector<Pending> pending;   // deferred fires in flight
-    for (int s = 0; s < h->G && e == cudaSuccess; ++s) {
-        const int ph = s & (h->H - 1);
+    cudaEvent_t sp_last = nullptr;  // completion of the newest side spread launch
+    for (int s = 0; s < h->G && e == cudaSuccess; s += h->KB) {   // s: first base step of the step
+        const int ph = phase_of(h, s);
         // deferred fires whose output this step emits join the chain here
         for (size_t i = 0; i < pending.size() && e == cudaSuccess;) {
             if (pending[i].due_step <= s) {
@@ -293,6 +316,19 @@ int build_graph(pc_handle* h) {
             } else {
                 ++i;
             }
+        }
+        // levels' spread tasks (several base blocks per step): their own branch,
+        // waited for only by the levels' deferred fires and the graph's end
+        if (h->sp_cnt[ph] > 0 && e == cudaSuccess) {
+            cudaEvent_t fork = mk();
+            e = cudaEventRecord(fork, h->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->sside, fork, 0);
+            if (e == cudaSuccess)
+                e = launch_side_spreads(h->sp_cnt[ph], h->d_tasks + h->sp_off[ph], dummy, h->d_rs, s, h->sside);
+            cudaEvent_t done = mk();
+            if (e == cudaSuccess) e = cudaEventRecord(done, h->sside);
+            sp_last = done;
+            ++kernels;
         }
         std::vector<cudaEvent_t> joins;
         for (int cls = 0; cls < kClasses && e == cudaSuccess; ++cls) {
@@ -323,6 +359,7 @@ int build_graph(pc_handle* h) {
             cudaEvent_t fork = mk();
             e = cudaEventRecord(fork, h->stream);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(h->aside[gr.cls], fork, 0);
+            if (e == cudaSuccess && sp_last) e = cudaStreamWaitEvent(h->aside[gr.cls], sp_last, 0);
             // a large deferred fire takes a whole SM (shared memory), so it
             // never shares one with the step chain's kernels
             if (e == cudaSuccess)
@@ -330,7 +367,7 @@ int build_graph(pc_handle* h) {
                                       h->d_rs, s, h->aside[gr.cls], false, -1, gr.cls != h->l0_class);
             cudaEvent_t done = mk();
             if (e == cudaSuccess) e = cudaEventRecord(done, h->aside[gr.cls]);
-            pending.push_back({s + gr.due, done});
+            pending.push_back({s + gr.due * h->KB, done});
             ++kernels;
         }
     }
@@ -338,6 +375,7 @@ int build_graph(pc_handle* h) {
     // overlap the next one's state update)
     for (auto& pd : pending)
         if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, pd.done, 0);
+    if (sp_last && e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, sp_last, 0);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     for (auto ev : evs) cudaEventDestroy(ev);
     if (e == cudaSuccess) e = e2;
@@ -372,6 +410,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     CK(cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_greatest), "stream create");
     for (auto& s : h->side) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_greatest), "stream create");
     for (auto& s : h->aside) CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_least), "stream create");
+    CK(cudaStreamCreateWithPriority(&h->sside, cudaStreamNonBlocking, prio_least), "stream create");
     CK(prepare_kernels(), "kernel attributes");
 
     h->fs = fs;
@@ -392,6 +431,15 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->G = std::max(Hh, kMinGraphSteps);
     h->maxN = maxN;
     h->l0_class = fire_class_of(N0);
+    // base blocks per step: at most what the level-0 kernel supports, and
+    // every level >= 1 must span a whole number of steps
+    int KB = std::min(h->req_kb, max_step_blocks(N0));
+    for (auto& p : h->specs)
+        for (size_t L = 1; L < p.N.size(); ++L)
+            while (KB > 1 && (p.N[L] / N0) % KB) KB >>= 1;
+    h->KB = KB;
+    h->Hs = std::max(1, Hh / KB);
+    h->G = std::max(h->G, KB);
 
     // ---- arena layout --------------------------------------------------------------
     Carve cv;
@@ -435,19 +483,34 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     // w = min(slack, T - 2) steps so that it is joined before the level's
     // next block completes (the spreads of the block after next read its
     // spectrum).  Its window stays in the input ring meanwhile.
-    std::vector<int> rin(npc), rl(nlv), dwin(nlv, 0);
+    //
+    // With KB > 1 base blocks per step every level >= 1 is deferred: its
+    // block completes inside some step S, its fire is launched after S and
+    // joined w' + 1 steps later, w' = min(floor(slack / KB), N_L / (KB N0) - 1).
+    // The first output sample is due at the start of step S + floor(slack /
+    // KB) + 1 (outputs of a level block start on a multiple of N_L, a
+    // multiple of KB N0), and the cap keeps the fire ahead of the spreads of
+    // the block after next.
+    // dfl: the level runs in the deferred form (parts >= 2 from double-buffered rows).
+    std::vector<int> rin(npc), rl(nlv), dwin(nlv, 0), dfl(nlv, 0);
     {
         int li = 0;
         for (int i = 0; i < npc; ++i) {
             const PCSpec& p = h->specs[i];
-            long need = 2L * p.N.back();
+            long need = std::max(2L * p.N.back(), (long)(KB + 1) * N0);
             long sacc = 0;
             for (size_t L = 0; L < p.N.size(); ++L, ++li) {
                 const long T = p.N[L] / N0, sb = sacc / N0;
-                if (L > 0 && T >= 4) {
+                if (L > 0 && KB > 1) {
+                    const long w = std::min((sb - T) / KB, T / KB - 1);
+                    dwin[li] = (int)w;
+                    dfl[li] = 1;
+                    need = std::max(need, 2L * p.N[L] + (w + 1) * (long)KB * N0);
+                } else if (L > 0 && T >= 4) {
                     const long w = std::min(sb - T, T - 2);
                     if (w >= 1) {
                         dwin[li] = (int)w;
+                        dfl[li] = 1;
                         need = std::max(need, 2L * p.N[L] + (w + 1) * (long)N0);
                     }
                 }
@@ -464,7 +527,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             long s = 0;
             for (size_t L = 0; L < p.N.size(); ++L, ++li) {
                 long r = p.N[L];
-                while (r < s + N0) r <<= 1;
+                while (r < s + (long)KB * N0) r <<= 1;
                 rl[li] = (int)r;
                 s += (long)p.N[L] * p.P[L];
             }
@@ -500,8 +563,8 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 l.cs = p.N[L] + 2;
                 l.rmask = rl[li] - 1;
                 l.pc = i;
-                {   // spread tasks sum parts >= 2 (level 0, deferred levels) or >= 1
-                    const int p_lo = (L == 0 || dwin[li] > 0) ? 2 : 1;
+                {   // spread tasks sum parts >= 2 KB (level 0), >= 2 (deferred levels) or >= 1
+                    const int p_lo = L == 0 ? 2 * KB : (dfl[li] ? 2 : 1);
                     const int np = p.P[L] - p_lo;
                     l.npart = np > 0 ? (np + spread_task_parts() - 1) / spread_task_parts() : 1;
                 }
@@ -513,16 +576,19 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     // ---- per (class, phase) task lists ------------------------------------------------
     // Tasks point into the arena, so they are built after the state offsets
     // are known; first count them to size the table.
-    std::vector<std::vector<std::vector<Task>>> lists(kClasses, std::vector<std::vector<Task>>(Hh));
+    const int NP = h->Hs;   // phases
+    std::vector<std::vector<std::vector<Task>>> lists(kClasses, std::vector<std::vector<Task>>(NP));
     std::map<std::tuple<int, int, int>, std::vector<Task>> dlists;   // (phase, due, class) -> deferred fires
     std::map<std::tuple<int, int, int>, double> dbytes;
-    for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(Hh, 0.0);
+    std::vector<std::vector<Task>> sp_lists(NP);   // side spread tasks per phase (KB > 1)
+    h->sp_bytes.assign(NP, 0.0);
+    for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(NP, 0.0);
     // order: larger fires first (longest CTAs start first), then level-0
     // fires, then spread tasks
     std::vector<int> order(nlv);
     for (int i = 0; i < nlv; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h->h_lv[a].N > h->h_lv[b].N; });
-    for (int g = 0; g < Hh; ++g) {
+    for (int g = 0; g < NP && KB == 1; ++g) {
         for (int li : order) {
             const DevLevel& l = h->h_lv[li];
             if ((g + 1 + l.s_blocks) % l.T) continue;
@@ -617,19 +683,127 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             h->alg_bytes[sc][g] += (16.0 * (l.P - p_lo) + 8.0 * l.npart) * (hi - lo);
         }
     }
+    // Several base blocks per step (KB > 1): step S covers base steps
+    // S KB .. S KB + KB - 1 and has phase S mod NP (every level's pattern
+    // repeats every N_L / (KB N0) steps, which divides NP).  A task sees the
+    // base step c = S KB - origin.
+    for (int g = 0; g < NP && KB > 1; ++g) {
+        const long long S = g, c0 = S * KB;
+        auto fire_task = [&](int li) {
+            const DevLevel& l = h->h_lv[li];
+            const DevPC& d = h->h_pcs[l.pc];
+            Task t{};
+            t.kind = 0;
+            t.N = l.N;
+            t.logN = l.logN;
+            t.P = l.P;
+            t.T = l.T;
+            t.s_blocks = l.s_blocks;
+            t.cs = l.cs;
+            t.rmask = l.rmask;
+            t.M = d.M;
+            t.in_ch = d.in_ch;
+            t.out_ch = d.out_ch;
+            t.mix_mode = d.mix_mode;
+            t.zero_outs = (l.T == 1) ? d.zero_outs : 0;
+            t.zero_off = d.zero_off;
+            t.rin_mask = d.rin_mask;
+            t.lv_index = li;
+            t.scale = d.scale;
+            return t;
+        };
+        for (int li : order) {
+            const DevLevel& l = h->h_lv[li];
+            const DevPC& d = h->h_pcs[l.pc];
+            const double C = l.N + 1.0;
+            const int cls = fire_class_of(l.N);
+            if (l.T == 1) {   // level 0: KB blocks, parts < 2 KB in the fire
+                Task t = fire_task(li);
+                const int Q = std::min(l.P, 2 * KB);
+                const int rows = l.P > 2 * KB ? l.npart : 0;
+                t.k0 = rows;
+                // per block: H_0 read and the new X row written, Q - 1 older
+                // (H, X) row pairs, the partial-sum rows, 2N window samples read
+                // and N written, the other levels' due slices, the ring append
+                const double b = 16.0 * C * Q + 8.0 * C * rows + 12.0 * l.N + 4.0 * N0 * (d.M - 1) + 4.0 * N0;
+                lists[cls][g].push_back(t);
+                h->alg_bytes[cls][g] += KB * b;
+                continue;
+            }
+            // the level's block that completes within this step, if any
+            const long long r = (c0 + 1 + l.s_blocks) % l.T;
+            const long long cb = c0 + (r == 0 ? 0 : l.T - r);
+            if (cb >= c0 + KB) continue;
+            Task t = fire_task(li);
+            t.k0 = l.npart;
+            t.dfer = 1;
+            t.origin = -(cb - c0);
+            const double b =
+                16.0 * C + 12.0 * l.N + 8.0 * C * (l.P >= 2 ? 2.0 : 0.0) + (l.P >= 3 ? 8.0 * C * l.npart : 0.0);
+            dlists[std::make_tuple(g, dwin[li] + 1, cls)].push_back(t);
+            dbytes[std::make_tuple(g, dwin[li] + 1, cls)] += b;
+        }
+        const int sc = h->l0_class;
+        for (int li = 0; li < nlv; ++li) {
+            const DevLevel& l = h->h_lv[li];
+            auto add_spreads = [&](int lo, int hi, int p_lo, long long origin, std::vector<Task>& dst, double& bytes,
+                                   double blocks) {
+                for (int k0 = lo; k0 < hi; k0 += spread_task_bins())
+                    for (int q = 0; q < l.npart; ++q) {   // parts [p_lo + 16 q, p_lo + 16 (q + 1)) into row q
+                        Task t{};
+                        t.kind = 1;
+                        t.N = l.N;
+                        t.P = l.P;
+                        t.T = l.T;
+                        t.s_blocks = l.s_blocks;
+                        t.cs = l.cs;
+                        t.k0 = k0;
+                        t.k1 = std::min(hi, k0 + spread_task_bins());
+                        t.p_lo = p_lo + q * spread_task_parts();
+                        t.in_ch = std::min(l.P, p_lo + (q + 1) * spread_task_parts());
+                        t.out_ch = q;
+                        t.lv_index = li;
+                        t.dfer = l.T > 1;
+                        t.origin = origin;
+                        dst.push_back(t);
+                    }
+                bytes += blocks * (16.0 * (l.P - p_lo) + 8.0 * l.npart) * (hi - lo);
+            };
+            if (l.T == 1) {   // parts >= 2 KB of the next step's blocks S KB + KB .. S KB + 2 KB - 1
+                if (l.P <= 2 * KB) continue;
+                add_spreads(0, l.cs, 2 * KB, -(long long)(KB - 1), lists[sc][g], h->alg_bytes[sc][g], KB);
+                continue;
+            }
+            if (l.P < 3) continue;
+            // parts >= 2 of the first block completing at or after this step's
+            // start, in N_L / (KB N0) slices over the steps after the step in
+            // which its predecessor completed
+            const long long bt = (c0 + l.s_blocks) / l.T;
+            const long long sprev = floordiv(bt * l.T - l.s_blocks - 1, KB);
+            const int nch = l.T / KB;
+            const long long j = S - 1 - sprev;
+            if (j < 0 || j >= nch) {
+                free_device(h);
+                return fail(h, PC_ERR_STATE, "internal: spread slice out of range");
+            }
+            const int lo = (int)((j * l.cs / nch) & ~1LL);
+            const int hi = (j == nch - 1) ? l.cs : (int)(((j + 1) * l.cs / nch) & ~1LL);
+            add_spreads(lo, hi, 2, 1, sp_lists[g], h->sp_bytes[g], 1.0);
+        }
+    }
     size_t ntasks = 0;
     for (int cls = 0; cls < kClasses; ++cls) {
-        h->off[cls].assign(Hh + 1, 0);
-        h->cnt[cls].assign(Hh, 0);
-        for (int g = 0; g < Hh; ++g) {
+        h->off[cls].assign(NP + 1, 0);
+        h->cnt[cls].assign(NP, 0);
+        for (int g = 0; g < NP; ++g) {
             h->off[cls][g] = (int)ntasks;
             h->cnt[cls][g] = (int)lists[cls][g].size();
             ntasks += lists[cls][g].size();
         }
-        h->off[cls][Hh] = (int)ntasks;
+        h->off[cls][NP] = (int)ntasks;
     }
     h->dgroups.clear();
-    h->dg_of_phase.assign(Hh, {});
+    h->dg_of_phase.assign(NP, {});
     for (auto& kv : dlists) {
         pc_handle::DGroup gr;
         gr.phase = std::get<0>(kv.first);
@@ -642,6 +816,13 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         h->dgroups.push_back(gr);
         ntasks += kv.second.size();
     }
+    h->sp_off.assign(NP, 0);
+    h->sp_cnt.assign(NP, 0);
+    for (int g = 0; g < NP; ++g) {
+        h->sp_off[g] = (int)ntasks;
+        h->sp_cnt[g] = (int)sp_lists[g].size();
+        ntasks += sp_lists[g].size();
+    }
     const size_t off_tasks = cv.take(sizeof(Task) * std::max<size_t>(1, ntasks));
 
     // state region
@@ -650,7 +831,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     so.pcout.resize(npc);
     for (int i = 0; i < npc; ++i) {
         so.xring[i] = cv.take(sizeof(float) * rin[i]);
-        so.pcout[i] = cv.take(sizeof(float) * N0);
+        so.pcout[i] = cv.take(sizeof(float) * N0 * KB);
     }
     so.X.resize(nlv);
     so.Yp.resize(nlv);
@@ -658,7 +839,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     for (int li = 0; li < nlv; ++li) {
         const DevLevel& l = h->h_lv[li];
         so.X[li] = cv.take(sizeof(float2) * (size_t)l.P * l.cs);
-        so.Yp[li] = cv.take(sizeof(float2) * 2 * (size_t)l.npart * l.cs);
+        so.Yp[li] = cv.take(sizeof(float2) * 2 * (l.T == 1 ? KB : 1) * (size_t)l.npart * l.cs);
         so.yr[li] = cv.take(sizeof(float) * (size_t)(l.rmask + 1));
     }
     so.mix = cv.take(sizeof(int) * n_out);
@@ -693,8 +874,9 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     all_tasks.reserve(ntasks);
     std::vector<const std::vector<Task>*> in_order;
     for (int cls = 0; cls < kClasses; ++cls)
-        for (int g = 0; g < Hh; ++g) in_order.push_back(&lists[cls][g]);
+        for (int g = 0; g < NP; ++g) in_order.push_back(&lists[cls][g]);
     for (auto& kv : dlists) in_order.push_back(&kv.second);
+    for (int g = 0; g < NP; ++g) in_order.push_back(&sp_lists[g]);
     for (const auto* lst : in_order)
             for (Task t : *lst) {
                 const DevLevel& l = h->h_lv[t.lv_index];
@@ -767,6 +949,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->bank.W = reinterpret_cast<const float2*>(A + off_W);
     h->bank.wlog = kWlog;
     h->bank.N0 = N0;
+    h->bank.kb = KB;
     h->bank.n_out = n_out;
     h->bank.out_off = reinterpret_cast<const int*>(A + off_out_off);
     h->bank.out_pcs = reinterpret_cast<const int*>(A + off_out_pcs);
@@ -884,7 +1067,7 @@ int run_steps(pc_handle* h, const IOView& view, long long nsteps, cudaStream_t s
     rs.io = view;
     bool first = true;   // the stream's preceding work is not a step kernel
     auto direct = [&](long long upto) -> int {
-        for (; done < upto; ++done) {
+        for (; done < upto; done += h->KB) {
             rs.step_base = h->frame_num + done;
             int r = launch_step_direct(h, rs, st, first);
             if (r) return r;
@@ -935,8 +1118,10 @@ __global__ void relaxed_carry_kernel(float* carry, const float* res, long long f
 int process_device_impl(pc_handle* h, float* d_out, const float* d_in, long long frames, int layout,
                         cudaStream_t st) {
     if (!h->ready) return fail(h, PC_ERR_STATE, "process before setup");
-    if (!d_out || !d_in || frames <= 0 || frames % h->N0)
-        return fail(h, PC_ERR_ARG, "frames must be a positive multiple of buffer_size");
+    if (!d_out || !d_in || frames <= 0 || frames % ((long long)h->N0 * h->KB))
+        return fail(h, PC_ERR_ARG, h->KB > 1 ? "frames must be a positive multiple of buffer_size x step blocks (" +
+                                                   std::to_string(h->KB) + ")"
+                                             : std::string("frames must be a positive multiple of buffer_size"));
     if (layout != PC_INTERLEAVED && layout != PC_PLANAR) return fail(h, PC_ERR_ARG, "unknown layout");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
     const long long nsteps = frames / h->N0;
@@ -1060,6 +1245,14 @@ int pc_setup_config(pc_handle* h, const char* config_file, int max_threads_per_l
     return do_setup(h, cfg.fs, cfg.buffer_size, cfg.n_in, cfg.n_out, std::move(specs));
 }
 
+int pc_set_step_blocks(pc_handle* h, int k) {
+    if (!h) return PC_ERR_ARG;
+    if (h->ready) return fail(h, PC_ERR_STATE, "step blocks must be set before setup");
+    if (k < 1 || k > 8 || (k & (k - 1))) return fail(h, PC_ERR_ARG, "step blocks must be 1, 2, 4 or 8");
+    h->req_kb = k;
+    return PC_OK;
+}
+
 int pc_set_relaxed(pc_handle* h, int relaxed) {
     if (!h) return PC_ERR_ARG;
     h->relaxed = relaxed ? 1 : 0;
@@ -1074,6 +1267,9 @@ int pc_run(pc_handle* h, float* output, const float* input, int frame_count) {
     if (frame_count != h->N0)
         return fail(h, PC_ERR_ARG,
                     "frameCount (" + std::to_string(frame_count) + ") != buffer_size (" + std::to_string(h->N0) + ")");
+    if (h->KB > 1)
+        return fail(h, PC_ERR_STATE, "run() processes one block; this handle computes " + std::to_string(h->KB) +
+                                         " blocks per step (use process)");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
     const size_t in_b = sizeof(float) * (size_t)h->N0 * h->n_in, out_b = sizeof(float) * (size_t)h->N0 * h->n_out;
     std::memcpy(h->h_in1, input, in_b);
@@ -1089,8 +1285,8 @@ int pc_run(pc_handle* h, float* output, const float* input, int frame_count) {
 int pc_process(pc_handle* h, float* output, const float* input, long long frames, int layout) {
     if (!h) return PC_ERR_ARG;
     if (!h->ready) return fail(h, PC_ERR_STATE, "process before setup");
-    if (!output || !input || frames <= 0 || frames % h->N0)
-        return fail(h, PC_ERR_ARG, "frames must be a positive multiple of buffer_size");
+    if (!output || !input || frames <= 0 || frames % ((long long)h->N0 * h->KB))
+        return fail(h, PC_ERR_ARG, "frames must be a positive multiple of buffer_size x step blocks");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
     const size_t nin = (size_t)frames * h->n_in, nout = (size_t)frames * h->n_out;
     if (nin > h->big_in_cap) {
@@ -1158,6 +1354,7 @@ int pc_get_info(const pc_handle* h, pc_info* info) {
     info->max_block_size = h->maxN;
     info->relaxed = h->relaxed;
     info->hyperperiod = h->H;
+    info->step_blocks = h->KB;
     info->frame_num = h->frame_num;
     info->device_bytes =
         (long long)h->arena_bytes + (long long)sizeof(float) * (h->big_in_cap + h->big_out_cap + h->rtmp_cap);
@@ -1182,7 +1379,8 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     if (!h->ready) return fail(h, PC_ERR_STATE, "profile before setup");
     if (nsteps < 1 || !out || max_kinds < 1) return fail(h, PC_ERR_ARG, "bad profile arguments");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
-    static const char* names[kClasses] = {"step_small", "step_mid", "step_large"};
+    constexpr int kKinds = kClasses + 1;   // + the side spread launches
+    static const char* names[kKinds] = {"step_small", "step_mid", "step_large", "spread_side"};
     struct Rec {
         int cls;
         int phase;
@@ -1197,9 +1395,21 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     RunState rs;
     rs.io = v;
     int rc = PC_OK;
-    for (long long s = 0; s < nsteps && rc == PC_OK; ++s) {
+    nsteps = (nsteps + h->KB - 1) / h->KB * h->KB;   // whole steps of KB base blocks
+    for (long long s = 0; s < nsteps && rc == PC_OK; s += h->KB) {
         rs.step_base = h->frame_num + s;
         const int ph = phase_of(h, rs.step_base);
+        if (h->sp_cnt[ph] > 0) {
+            Rec r{kClasses, ph, -1, nullptr, nullptr};
+            cudaEventCreate(&r.a);
+            cudaEventCreate(&r.b);
+            cudaEventRecord(r.a, h->stream);
+            cudaError_t e = launch_side_spreads(h->sp_cnt[ph], h->d_tasks + h->sp_off[ph], rs, nullptr, 0, h->stream);
+            cudaEventRecord(r.b, h->stream);
+            recs.push_back(r);
+            h->launches += 1;
+            if (e != cudaSuccess) rc = cuda_fail(h, e, "profile launch");
+        }
         for (int k = 0; k < kClasses && rc == PC_OK; ++k) {
             const int cls = (h->l0_class + k) % kClasses;
             const int n = h->cnt[cls][ph];
@@ -1232,13 +1442,14 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     }
     h->frame_num += nsteps;
     cudaError_t se = cudaStreamSynchronize(h->stream);
-    double ms[kClasses] = {0, 0, 0}, bytes[kClasses] = {0, 0, 0};
-    long long cnt[kClasses] = {0, 0, 0};
+    double ms[kKinds] = {0, 0, 0, 0}, bytes[kKinds] = {0, 0, 0, 0};
+    long long cnt[kKinds] = {0, 0, 0, 0};
     for (auto& r : recs) {
         float t = 0.f;
         if (se == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
             ms[r.cls] += t;
-            bytes[r.cls] += r.dgroup < 0 ? h->alg_bytes[r.cls][r.phase] : h->dgroups[r.dgroup].bytes;
+            bytes[r.cls] += r.cls == kClasses ? h->sp_bytes[r.phase]
+                                              : (r.dgroup < 0 ? h->alg_bytes[r.cls][r.phase] : h->dgroups[r.dgroup].bytes);
             cnt[r.cls] += 1;
         }
         cudaEventDestroy(r.a);
@@ -1247,8 +1458,8 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     if (rc) return rc;
     if (se != cudaSuccess) return cuda_fail(h, se, "profile sync");
     int n = 0;
-    for (int k = 0; k < kClasses && n < max_kinds; ++k) {
-        const int cls = (h->l0_class + k) % kClasses;
+    for (int k = 0; k < kKinds && n < max_kinds; ++k) {
+        const int cls = k < kClasses ? (h->l0_class + k) % kClasses : kClasses;
         if (cnt[cls] == 0) continue;
         std::snprintf(out[n].name, sizeof out[n].name, "%s", names[cls]);
         out[n].launches = cnt[cls];

@@ -5,7 +5,8 @@
 //   per PC:    input ring xring[Rin]           (time domain, Rin = pow2 >= 2 N_max)
 //   per level: H[P][cs]  filter spectra        (float2, cs = N + 2 row stride)
 //              X[P][cs]  input-spectrum ring   (slot b mod P holds block b)
-//              Yp[2][cs] partial sums of the FDL MAC for the next block
+//              Yp[rows][2][cs] partial sums of the FDL MAC for the next block
+//                        (level 0 with K base blocks per step: [rows][2K][cs])
 //              yring[R]  output ring            (levels >= 1; R = pow2 >= s_L + N0)
 //   per PC:    pcout[N0] level sum (only when an output mixes several PCs)
 //   global:    twiddle table W[2^wlog], per-phase task tables, mix counters.
@@ -33,7 +34,8 @@ struct DevLevel {
     int npart;      // partial-sum rows (spread tasks cover at most kSpreadParts parts each)
     float2* H;      // [P][cs]
     float2* X;      // [P][cs]
-    float2* Yp;     // [npart][2][cs]: row q, block parity
+    float2* Yp;     // [npart][2][cs]: row q, block parity ([npart][2K][cs], block mod 2K, for
+                    // level 0 with K base blocks per step)
     float* yring;   // [rmask + 1]
 };
 
@@ -67,7 +69,10 @@ struct Task {
     int rin_mask, lv_index, p_lo, active;   // p_lo: first part summed by a spread task
     float scale;
     int dfer;           // 1: the level's fire runs off the step chain (deferred), see engine.cu
-    long long origin;   // step at which this PC's time starts (0 for a static bank)
+    // step at which this PC's time starts (serving pools); in a static bank
+    // with several base blocks per step, minus the offset of the task's base
+    // step within the launch's step (a task sees c = launch step - origin)
+    long long origin;
     float2* H;
     float2* X;
     float2* Yp;
@@ -111,7 +116,7 @@ struct Bank {
     int wlog;
     int N0;
     int n_out;
-    int pad;
+    int kb;                // base blocks per step (level-0 sub-blocks of one fire); 0 or 1: one
     // per output channel mixing lists (mix_mode 2): out_off[o]..out_off[o+1]
     const int* out_off;
     const int* out_pcs;

@@ -31,16 +31,24 @@ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 
+// Placement of quarter-wave table entry m (< 2^15) in its conflict-free
+// form: the low four bits XORed with the three nibbles above them, so 16
+// threads reading entries k 2^s (k consecutive, any s), or 16 consecutive
+// entries, hit distinct 8-byte bank pairs.
+__device__ __forceinline__ int twsw(int m) { return m ^ (((m >> 4) ^ (m >> 8) ^ (m >> 12)) & 15); }
+
 // Quarter-wave twiddle table of a 2N-point circle in shared memory.
 struct Twiddles {
-    const float2* tab;   // N/2 entries
+    const float2* tab;   // N/2 entries (entry m at tab[twsw(m)] when read with SW)
     int logN;            // log2 N
 
     // exp(-+2 pi i a / 2^lg), 0 <= a < 2^lg, 2^lg <= 2N
+    template <bool SW = false>
     __device__ __forceinline__ float2 get(int a, int lg, bool inv) const {
         const int a2 = a << (logN + 1 - lg);           // index on the 2N circle
         const int q = a2 >> (logN - 1);                // quadrant
-        const float2 t = tab[a2 & ((1 << (logN - 1)) - 1)];
+        const int m = a2 & ((1 << (logN - 1)) - 1);
+        const float2 t = tab[SW ? twsw(m) : m];
         // quadrant q rotates by (-i)^q: odd q swaps (x, y) -> (y, -x), q >= 2 negates
         // (selects rather than a switch, so a warp does not diverge)
         const bool odd = (q & 1) != 0;
@@ -59,8 +67,20 @@ __device__ __forceinline__ void load_twiddles(float2* tab, int logN, const float
     for (int m = threadIdx.x; m < n; m += NT) tab[m] = __ldg(&W[m << sh]);
 }
 
+// Shared-memory placement of complex element i of a transform buffer.  With
+// SW the low four bits of i are XORed with 5 * ((i >> 4) & 3): a bijection
+// on every block of 64 elements under which the strided writes of the first
+// stages (elements 4j + r, and 16m + k + 4r, of consecutive threads j) and
+// every aligned run of 16 elements hit 16 distinct 8-byte bank pairs, so a
+// half-warp's 64-bit accesses have no bank conflicts.  Every access to a
+// buffer must use the same placement.
+template <bool SW>
+__device__ __forceinline__ int sidx(int i) {
+    return SW ? (i ^ (((i >> 4) & 3) * 5)) : i;
+}
+
 // One radix-4 Stockham stage (Ns = product of previous radices).
-template <int NT, int MAXB>
+template <int NT, int MAXB, bool SW = false>
 __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, const Twiddles& tw, bool inv) {
     const int nb = N >> 2;
     float2 v[MAXB][4];
@@ -69,7 +89,7 @@ __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, con
         const int j = threadIdx.x + i * NT;
         if (j < nb) {
 #pragma unroll
-            for (int r = 0; r < 4; ++r) v[i][r] = s[j + r * nb];
+            for (int r = 0; r < 4; ++r) v[i][r] = s[sidx<SW>(j + r * nb)];
         }
     }
     __syncthreads();
@@ -80,9 +100,9 @@ __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, con
             const int k = j & (Ns - 1);
             if (Ns > 1) {
                 const int lg = lgNs + 2;
-                v[i][1] = cmul(v[i][1], tw.get(k, lg, inv));
-                v[i][2] = cmul(v[i][2], tw.get(2 * k, lg, inv));
-                v[i][3] = cmul(v[i][3], tw.get(3 * k, lg, inv));
+                v[i][1] = cmul(v[i][1], tw.get<SW>(k, lg, inv));
+                v[i][2] = cmul(v[i][2], tw.get<SW>(2 * k, lg, inv));
+                v[i][3] = cmul(v[i][3], tw.get<SW>(3 * k, lg, inv));
             }
             const float2 a0 = cadd(v[i][0], v[i][2]);
             const float2 a1 = csub(v[i][0], v[i][2]);
@@ -91,17 +111,17 @@ __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, con
             // forward: (v1 - v3) * (-i); inverse: (v1 - v3) * (+i)
             const float2 a3 = inv ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
             const int base = ((j - k) << 2) + k;
-            s[base] = cadd(a0, a2);
-            s[base + Ns] = cadd(a1, a3);
-            s[base + 2 * Ns] = csub(a0, a2);
-            s[base + 3 * Ns] = csub(a1, a3);
+            s[sidx<SW>(base)] = cadd(a0, a2);
+            s[sidx<SW>(base + Ns)] = cadd(a1, a3);
+            s[sidx<SW>(base + 2 * Ns)] = csub(a0, a2);
+            s[sidx<SW>(base + 3 * Ns)] = csub(a1, a3);
         }
     }
     __syncthreads();
 }
 
 // Final radix-2 Stockham stage.
-template <int NT, int MAXB>
+template <int NT, int MAXB, bool SW = false>
 __device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, const Twiddles& tw, bool inv) {
     const int nb = N >> 1;
     float2 v[2 * MAXB][2];
@@ -109,8 +129,8 @@ __device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, con
     for (int i = 0; i < 2 * MAXB; ++i) {
         const int j = threadIdx.x + i * NT;
         if (j < nb) {
-            v[i][0] = s[j];
-            v[i][1] = s[j + nb];
+            v[i][0] = s[sidx<SW>(j)];
+            v[i][1] = s[sidx<SW>(j + nb)];
         }
     }
     __syncthreads();
@@ -120,23 +140,24 @@ __device__ __forceinline__ void stage_r2(float2* s, int N, int Ns, int lgNs, con
         if (j < nb) {
             const int k = j & (Ns - 1);
             float2 b = v[i][1];
-            if (Ns > 1) b = cmul(b, tw.get(k, lgNs + 1, inv));
+            if (Ns > 1) b = cmul(b, tw.get<SW>(k, lgNs + 1, inv));
             const int base = ((j - k) << 1) + k;
-            s[base] = cadd(v[i][0], b);
-            s[base + Ns] = csub(v[i][0], b);
+            s[sidx<SW>(base)] = cadd(v[i][0], b);
+            s[sidx<SW>(base + Ns)] = csub(v[i][0], b);
         }
     }
     __syncthreads();
 }
 
-// In-place complex FFT of N = 2^logN points in shared memory (unnormalised).
-// Requires N / 4 <= NT * MAXB and 16 <= N.  Callers __syncthreads() after
-// writing the data; the function ends with a barrier.
-template <int NT, int MAXB>
+// In-place complex FFT of N = 2^logN points in shared memory (unnormalised),
+// element i at s[sidx<SW>(i)].  Requires N / 4 <= NT * MAXB and 16 <= N.
+// Callers __syncthreads() after writing the data; the function ends with a
+// barrier.
+template <int NT, int MAXB, bool SW = false>
 __device__ void fft_smem(float2* s, int N, int logN, const Twiddles& tw, bool inv) {
     int Ns = 1, lgNs = 0;
-    for (; lgNs + 2 <= logN; lgNs += 2, Ns <<= 2) stage_r4<NT, MAXB>(s, N, Ns, lgNs, tw, inv);
-    if (lgNs < logN) stage_r2<NT, MAXB>(s, N, Ns, lgNs, tw, inv);
+    for (; lgNs + 2 <= logN; lgNs += 2, Ns <<= 2) stage_r4<NT, MAXB, SW>(s, N, Ns, lgNs, tw, inv);
+    if (lgNs < logN) stage_r2<NT, MAXB, SW>(s, N, Ns, lgNs, tw, inv);
 }
 
 // Radix-4 and radix-2 Stockham stages from src to dst (a second buffer): one
@@ -219,8 +240,97 @@ __device__ void fft_smem_pp(float2* s, float2* tmp, int N, int logN, const Twidd
     if (n2) stage_r2_pp<NT, MAXB>(a, b, N, Ns, lgNs, tw, inv);
 }
 
+// Batched Stockham stages: K transforms of N points, transform t at
+// src + t N (dst + t N); the stage's K N / 4 (radix 4) or K N / 2 (radix 2)
+// butterflies are dealt round-robin over the CTA, so a CTA with more
+// threads than one transform has butterflies keeps all of them busy.  Same
+// arithmetic per butterfly as the single-transform stages.
+template <int NT, int MAXB>
+__device__ __forceinline__ void stage_r4_batch(const float2* src, float2* dst, int K, int N, int logN, int Ns,
+                                               int lgNs, const Twiddles& tw, bool inv) {
+    const int nb = N >> 2;
+    const int total = K * nb;
+#pragma unroll
+    for (int i = 0; i < MAXB; ++i) {
+        const int jj = threadIdx.x + i * NT;
+        if (jj < total) {
+            const int t = jj >> (logN - 2);
+            const int j = jj & (nb - 1);
+            const float2* a = src + t * N;
+            float2* o = dst + t * N;
+            float2 v[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) v[r] = a[j + r * nb];
+            const int k = j & (Ns - 1);
+            if (Ns > 1) {
+                const int lg = lgNs + 2;
+                v[1] = cmul(v[1], tw.get(k, lg, inv));
+                v[2] = cmul(v[2], tw.get(2 * k, lg, inv));
+                v[3] = cmul(v[3], tw.get(3 * k, lg, inv));
+            }
+            const float2 a0 = cadd(v[0], v[2]);
+            const float2 a1 = csub(v[0], v[2]);
+            const float2 a2 = cadd(v[1], v[3]);
+            const float2 d = csub(v[1], v[3]);
+            const float2 a3 = inv ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+            const int base = ((j - k) << 2) + k;
+            o[base] = cadd(a0, a2);
+            o[base + Ns] = cadd(a1, a3);
+            o[base + 2 * Ns] = csub(a0, a2);
+            o[base + 3 * Ns] = csub(a1, a3);
+        }
+    }
+    __syncthreads();
+}
+
+template <int NT, int MAXB>
+__device__ __forceinline__ void stage_r2_batch(const float2* src, float2* dst, int K, int N, int logN, int Ns,
+                                               int lgNs, const Twiddles& tw, bool inv) {
+    const int nb = N >> 1;
+    const int total = K * nb;
+#pragma unroll
+    for (int i = 0; i < 2 * MAXB; ++i) {
+        const int jj = threadIdx.x + i * NT;
+        if (jj < total) {
+            const int t = jj >> (logN - 1);
+            const int j = jj & (nb - 1);
+            const float2* a = src + t * N;
+            float2* o = dst + t * N;
+            const float2 v0 = a[j];
+            float2 b = a[j + nb];
+            const int k = j & (Ns - 1);
+            if (Ns > 1) b = cmul(b, tw.get(k, lgNs + 1, inv));
+            const int base = ((j - k) << 1) + k;
+            o[base] = cadd(v0, b);
+            o[base + Ns] = csub(v0, b);
+        }
+    }
+    __syncthreads();
+}
+
+// K transforms of N points from buffer a into stages alternating between a
+// and b (both K N points); returns the buffer that holds the result.
+// Requires K N / 4 <= NT MAXB and 16 <= N.  Callers __syncthreads() after
+// writing the data; the function ends with a barrier.
+template <int NT, int MAXB>
+__device__ __noinline__ float2* fft_smem_batch(float2* a, float2* b, int K, int N, int logN, const Twiddles& tw, bool inv) {
+    int Ns = 1, lgNs = 0;
+    for (; lgNs + 2 <= logN; lgNs += 2, Ns <<= 2) {
+        stage_r4_batch<NT, MAXB>(a, b, K, N, logN, Ns, lgNs, tw, inv);
+        float2* t = a;
+        a = b;
+        b = t;
+    }
+    if (lgNs < logN) {
+        stage_r2_batch<NT, MAXB>(a, b, K, N, logN, Ns, lgNs, tw, inv);
+        a = b;
+    }
+    return a;
+}
+
 // Split post-pass for the pair (k, N-k), 0 <= k <= N/2, on Z = FFT_N(z).
 // Returns X[k] in xk and X[N-k] in xnk (for k == 0: X[0] and X[N]).
+template <bool SW = false>
 __device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int logN, const Twiddles& tw, float2& xk,
                                            float2& xnk) {
     if (k == 0) {
@@ -230,7 +340,7 @@ __device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int log
     }
     const float2 E = make_float2(0.5f * (zk.x + znk.x), 0.5f * (zk.y - znk.y));
     const float2 O = make_float2(0.5f * (zk.y + znk.y), -0.5f * (zk.x - znk.x));
-    const float2 w = tw.get(k, logN + 1, false);   // e^{-i pi k / N}
+    const float2 w = tw.get<SW>(k, logN + 1, false);   // e^{-i pi k / N}
     const float2 wO = cmul(w, O);
     xk = cadd(E, wO);
     xnk = cconj(csub(E, wO));
@@ -239,6 +349,7 @@ __device__ __forceinline__ void rfft_split(float2 zk, float2 znk, int k, int log
 // Inverse pre-pass for the pair (k, N-k) from Y[k] (yk) and Y[N-k] (ynk);
 // for k == 0 yk = Y[0], ynk = Y[N] and only zk (= Z'[0]) is meaningful.
 // Imaginary parts of Y[0] and Y[N] are ignored, as FFTW's c2r does.
+template <bool SW = false>
 __device__ __forceinline__ void irfft_merge(float2 yk, float2 ynk, int k, int logN, const Twiddles& tw, float2& zk,
                                             float2& znk) {
     if (k == 0) {
@@ -247,7 +358,7 @@ __device__ __forceinline__ void irfft_merge(float2 yk, float2 ynk, int k, int lo
     }
     const float2 A = make_float2(yk.x + ynk.x, yk.y - ynk.y);   // Y[k] + conj(Y[N-k])
     const float2 B = make_float2(yk.x - ynk.x, yk.y + ynk.y);   // Y[k] - conj(Y[N-k])
-    const float2 w = tw.get(k, logN + 1, false);
+    const float2 w = tw.get<SW>(k, logN + 1, false);
     const float2 cB = cmul(cconj(w), B);                          // conj(w^k) B
     zk = make_float2(A.x - cB.y, A.y + cB.x);                     // A + i conj(w^k) B
     const float2 wcB = cmul(w, cconj(B));                         // w^k conj(B)

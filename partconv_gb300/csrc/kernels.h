@@ -26,6 +26,12 @@ int class_threads(int cls);
 int spread_task_bins();
 int spread_task_parts();
 size_t class_smem_bytes(int cls, int maxN);
+// dynamic shared memory of a step launch (class, largest block, the bank's
+// base blocks per step)
+size_t step_smem_bytes(int cls, int maxN, const Bank& bank);
+// largest base-blocks-per-step K (a power of two <= 4) the level-0 kernel
+// supports for base block N0 (K N0 <= 1024); 1 if none
+int max_step_blocks(int N0);
 
 cudaError_t prepare_kernels();
 // pdl: let the launch overlap the previous kernel in the stream, which must
@@ -36,6 +42,9 @@ cudaError_t prepare_kernels();
 cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, const Task* tasks, const RunState& rs,
                               const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio = 0,
                               bool whole_sm = false);
+// spread tasks of levels >= 1 (several base blocks per step) as their own launch
+cudaError_t launch_side_spreads(int grid, const Task* tasks, const RunState& rs, const RunState* rs_dev,
+                                int step_in_batch, cudaStream_t st);
 cudaError_t launch_pool_class(int cls, int grid, int maxN, const Bank& bank, const Task* slots, const PoolCta* map,
                               const RunState& rs, cudaStream_t st);
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,

@@ -93,8 +93,9 @@ constexpr int kSpreadLanes = 64;   // threads per part-group: a task covers 128 
 // parts per spread task: one round of loads (4 groups x 4 in flight) per CTA
 constexpr int kSpreadParts = 16;
 
+// kb: base blocks per step (level 0 keeps 2 kb partial-sum buffers per row).
 template <int NT>
-__device__ __forceinline__ void spread_body(const Task& tk, long long c, float4* red) {
+__device__ __forceinline__ void spread_body(const Task& tk, long long c, float4* red, int kb) {
     constexpr int G = NT / kSpreadLanes;
     const int lane = threadIdx.x % kSpreadLanes;
     const int g = threadIdx.x / kSpreadLanes;
@@ -103,12 +104,13 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
     long long bt;      // block whose partial sum this step builds
     float2* dst;
     c -= tk.origin;    // the PC's own step count
-    const size_t row = (size_t)tk.out_ch * 2;   // partial-sum row, [row][parity][cs]
-    if (tk.T == 1) {   // level 0: parts p >= 2 of block c + 1
+    if (tk.T == 1) {   // level 0: parts p >= 2 kb of block c + 1, [row][block mod 2 kb][cs]
+        const int nbuf = 2 * kb;
         bt = c + 1;
-        dst = tk.Yp + (row + (size_t)(bt & 1)) * tk.cs;
+        dst = tk.Yp + ((size_t)tk.out_ch * nbuf + (size_t)(bt & (nbuf - 1))) * tk.cs;   // kb: a power of two
     } else {           // the block after the newest fired one: parts p >= 1, or
                        // p >= 2 (double-buffered) for a deferred level
+        const size_t row = (size_t)tk.out_ch * 2;   // [row][parity][cs]
         bt = (c + 1 + tk.s_blocks) / tk.T;
         dst = tk.Yp + (row + (tk.dfer ? (size_t)(bt & 1) : 0)) * tk.cs;
     }
@@ -154,6 +156,78 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
     }
 }
 
+// Level 0 with K base blocks per step: parts [p_lo, p_hi) of the next
+// step's K blocks bt_j = c + 1 + j (the task's c is the step's last base
+// step) over one slice of bins: each filter row is loaded once for the K
+// blocks.  Group g sums parts p_lo + g, p_lo + g + G, ...; groups are added
+// in order, per block.
+template <int NT, int KM>
+__device__ __forceinline__ void spread_multi(const Task& tk, long long c, float4* red) {
+    constexpr int G = NT / kSpreadLanes;
+    constexpr int U = 2;   // parts whose loads are in flight together
+    const int lane = threadIdx.x % kSpreadLanes;
+    const int g = threadIdx.x / kSpreadLanes;
+    const int k = tk.k0 + 2 * lane;
+    const bool active = k < tk.k1;
+    c -= tk.origin;
+    const long long bt0 = c + 1;
+    const int nbuf = 2 * KM;
+    const int P = tk.P;
+    const int p_hi = tk.in_ch > 0 ? tk.in_ch : P;
+    const size_t rs4 = (size_t)(tk.cs >> 1);
+    const float4* X4 = reinterpret_cast<const float4*>(tk.X + k);
+    const float4* H4 = reinterpret_cast<const float4*>(tk.H + k);
+    float4 acc[KM];
+#pragma unroll
+    for (int j = 0; j < KM; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+        const int Gm = G % P;
+        int sl0 = (int)imod(bt0 - (tk.p_lo + g), P);   // slot of block bt0 - p for the group's part p
+        for (int p0 = tk.p_lo + g; p0 < p_hi; p0 += U * G) {
+            float4 xv[U][KM], hv[U];
+            int sl = sl0;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (p0 + u * G < p_hi) {
+                    hv[u] = __ldg(H4 + (size_t)(p0 + u * G) * rs4);
+                    int sj = sl;
+#pragma unroll
+                    for (int j = 0; j < KM; ++j) {   // blocks bt0 + j - p: consecutive slots
+                        xv[u][j] = __ldcg(X4 + (size_t)sj * rs4);
+                        sj = (sj + 1 == P) ? 0 : sj + 1;
+                    }
+                }
+                sl -= Gm;
+                if (sl < 0) sl += P;
+            }
+            sl0 = sl;
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (p0 + u * G < p_hi) {
+#pragma unroll
+                    for (int j = 0; j < KM; ++j) acc[j] = f4mac(acc[j], xv[u][j], hv[u]);
+                }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < KM; ++j) {
+        float2* dst = tk.Yp + ((size_t)tk.out_ch * nbuf + (size_t)((bt0 + j) & (nbuf - 1))) * tk.cs;
+        if (G > 1) {
+            if (g > 0) red[(g - 1) * kSpreadLanes + lane] = acc[j];
+            __syncthreads();
+            if (g == 0 && active) {
+                float4 a = acc[j];
+#pragma unroll
+                for (int q = 1; q < G; ++q) a = f4add(a, red[(q - 1) * kSpreadLanes + lane]);
+                *reinterpret_cast<float4*>(dst + k) = a;
+            }
+            __syncthreads();   // red is reused for the next block
+        } else if (active) {
+            *reinterpret_cast<float4*>(dst + k) = acc[j];
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // EARLY (step kernels): a level-0 fire whose whole window lies in this
 // call's input runs its forward transform and forms X_b H_0 before waiting
@@ -163,6 +237,15 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
 // no kernel writes (input, twiddles, filter spectra) and writes only shared
 // memory, so it may overlap any number of earlier step kernels: it signals
 // its dependents at entry.
+// Output samples 4 i4 .. 4 i4 + 3 of a transform buffer (complex elements
+// 2 i4 and 2 i4 + 1, which sidx keeps in one aligned pair, possibly swapped).
+template <bool SW>
+__device__ __forceinline__ float4 ld_out4(const float2* s, int i4) {
+    const int p = sidx<SW>(2 * i4);
+    const float4 v = *reinterpret_cast<const float4*>(s + (p & ~1));
+    return (p & 1) ? make_float4(v.z, v.w, v.x, v.y) : v;
+}
+
 template <class C, bool EARLY>
 __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, const RunState& rs, long long c,
                                           float2* smem, int* s_last) {
@@ -183,10 +266,13 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     float* emit = reinterpret_cast<float*>(h0s + (N + 2));   // N0 floats (PREFETCH, level 0)
     float2* ftmp = reinterpret_cast<float2*>(emit + N);       // N complex FFT scratch (PREFETCH)
     const Twiddles tw{twt, logN};
+    // the large classes keep the transform buffer in the conflict-free
+    // placement (element i at s[sidx<SW>(i)])
+    constexpr bool SW = !C::PREFETCH;
     // prefetch classes transform through the scratch buffer (fewer barriers)
     auto fft = [&](bool inv) {
         if constexpr (C::PREFETCH) fft_smem_pp<NT, C::MAXB>(s, ftmp, N, logN, tw, inv);
-        else fft_smem<NT, C::MAXB>(s, N, logN, tw, inv);
+        else fft_smem<NT, C::MAXB, SW>(s, N, logN, tw, inv);
     };
 
     const long long io_step = c - rs.io.step0;   // I/O is addressed by the global step
@@ -285,14 +371,14 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         for (int i = 0; i < C::MAXQ; ++i) {
             const int qd = tid + i * NT;
             if ((qd >= nq_old || early) && qd < nq) {
-                s[2 * qd] = make_float2(wv[i].x, wv[i].y);
-                s[2 * qd + 1] = make_float2(wv[i].z, wv[i].w);
+                s[sidx<SW>(2 * qd)] = make_float2(wv[i].x, wv[i].y);
+                s[sidx<SW>(2 * qd + 1)] = make_float2(wv[i].z, wv[i].w);
             }
         }
 #pragma unroll
         for (int i = 0; i < C::MAXT; ++i) {
             const int m = tid + i * NT;
-            if (m < ntw) twt[m] = tv[i];
+            if (m < ntw) twt[SW ? twsw(m) : m] = tv[i];
         }
         if (C::PREFETCH) {
 #pragma unroll
@@ -437,32 +523,32 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             for (int i = 0; i < C::MAXQ; ++i) {
                 const int qd = tid + i * NT;
                 if (qd < nq_old) {
-                    s[2 * qd] = make_float2(wo[i].x, wo[i].y);
-                    s[2 * qd + 1] = make_float2(wo[i].z, wo[i].w);
+                    s[sidx<SW>(2 * qd)] = make_float2(wo[i].x, wo[i].y);
+                    s[sidx<SW>(2 * qd + 1)] = make_float2(wo[i].z, wo[i].w);
                 } else if (l0 && qd < nq) {   // append, read back from this thread's own writes
                     const long long ta = t_end - 2LL * N + 4LL * qd;
-                    const float2 a = s[2 * qd], bb = s[2 * qd + 1];
+                    const float2 a = s[sidx<SW>(2 * qd)], bb = s[sidx<SW>(2 * qd + 1)];
                     *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = make_float4(a.x, a.y, bb.x, bb.y);
                 }
             }
         }
         __syncthreads();
-        fft_smem<NT, C::MAXB>(s, N, logN, tw, false);
+        fft_smem<NT, C::MAXB, SW>(s, N, logN, tw, false);
 
         // ---- split, FDL MAC, inverse merge, operands streamed from L2 ----------
         auto finish_pair = [&](int k, float2 h0k, float2 h0nk, float2 ak, float2 ank) {
             const int nk = (k == 0) ? 0 : N - k;
             float2 xk, xnk;
-            rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
+            rfft_split<SW>(s[sidx<SW>(k)], s[sidx<SW>(nk)], k, logN, tw, xk, xnk);
             const int bk = k, bnk = N - k;   // k == 0 pairs bin 0 with bin N
             Xs[bk] = xk;
             if (bnk != bk) Xs[bnk] = xnk;
             const float2 yk = cadd(cmul(xk, h0k), ak);
             const float2 ynk = cadd(cmul(xnk, h0nk), ank);
             float2 zk, znk;
-            irfft_merge(yk, ynk, k, logN, tw, zk, znk);
-            s[k] = zk;
-            if (k != 0 && k != half) s[N - k] = znk;
+            irfft_merge<SW>(yk, ynk, k, logN, tw, zk, znk);
+            s[sidx<SW>(k)] = zk;
+            if (k != 0 && k != half) s[sidx<SW>(N - k)] = znk;
         };
         constexpr int CH = C::SPLIT_CH;
         for (int k0 = tid; k0 <= half; k0 += CH * NT) {
@@ -506,8 +592,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         // level block b covers output samples [b N, (b+1) N)
         const long long t0 = b * (long long)N;
         for (int i4 = tid; 4 * i4 < N; i4 += NT)
-            *reinterpret_cast<float4*>(tk.yring + ((t0 + 4 * i4) & tk.rmask)) =
-                reinterpret_cast<const float4*>(sf)[i4];
+            *reinterpret_cast<float4*>(tk.yring + ((t0 + 4 * i4) & tk.rmask)) = ld_out4<SW>(s, i4);
         return;
     }
 
@@ -515,7 +600,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     float* out = rs.io.out + io_step * rs.io.out_step;
     const long long osamp = rs.io.out_sample, och = rs.io.out_ch;
     for (int i = tid; i < N0; i += NT) {
-        float v = sf[i];
+        float v = SW ? reinterpret_cast<const float*>(s + sidx<SW>(i >> 1))[i & 1] : sf[i];
         if (C::PREFETCH) {
             if (tk.M > 1) v += emit[i];
         } else {
@@ -553,10 +638,311 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     if (tid == 0) bank.mix_cnt[o] = 0;
 }
 
+// 16-byte global -> shared copies that bypass the registers (L2-cached)
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// Level 0 over K base blocks per step (bank.kb = K > 1; offline processing
+// of many blocks per call): the CTA of one PC computes its blocks
+// b = c .. c + K - 1.  Block b + t sums X_{b+t-p} H_p over the parts
+// p < Q = min(P, 2K) here -- p <= t from this CTA's own forward transforms,
+// the others from the spectra ring -- and adds the partial-sum rows of the
+// parts p >= 2K that spread tasks built during the previous step (those read
+// only spectra of blocks <= b - 1).  Order: p ascending, then the rows in
+// order.  The K forward and K inverse transforms run as one batched
+// shared-memory FFT: a 256-point transform has 64 radix-4 butterflies per
+// stage, so four of them fill a 256-thread CTA for the cost of one.
+// Before the dependency wait the CTA reads only the call's input, twiddles
+// and filter rows and writes only shared memory, like the one-block fire.
+// ---------------------------------------------------------------------------
+constexpr int kMaxStepSamples = 1024;   // K N0 at most
+constexpr int kMaxStepBlocks = 4;       // K at most
+
+__host__ __device__ constexpr size_t multi_smem_bytes(int N, int K) {
+    // transform buffers 2 K N, twiddles N/2 (complex); filter rows 2K, spectra
+    // rows 3K - 1, sums K (rows of N + 2 complex); due output slices K N floats
+    return (size_t)8 * (2 * (size_t)K * N + (size_t)N / 2 + (size_t)(6 * K - 1) * (N + 2)) + (size_t)4 * K * N;
+}
+
+template <class C>
+__device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, const RunState& rs, long long c,
+                                           float2* smem, int* s_last) {
+    constexpr int NT = C::NT;
+    constexpr int MAXBB = (kMaxStepSamples / 4 + NT - 1) / NT;        // batched radix-4 butterflies per thread
+    constexpr int MAXI = (kMaxStepSamples / 2 + 8 + NT - 1) / NT;     // (block, bin pair) items per thread
+    constexpr int MAXW = (kMaxStepSamples / 4 + 128 + NT - 1) / NT;   // window quads per thread (K + 1 blocks)
+    constexpr int MAXE = (kMaxStepSamples / 4 + NT - 1) / NT;         // output quads per thread
+    const int tid = threadIdx.x;
+    const int K = bank.kb;
+    const int N = tk.N, logN = tk.logN, P = tk.P, cs = tk.cs;   // N = N0
+    const int half = N >> 1, ncol = cs >> 1;                     // ncol = half + 1 bin pairs (float4) per row
+    // item it < K half: block it >> (logN - 1), pair it & (half - 1); the
+    // K items after that: pair `half` (bins N, N + 1; the split's k = N/2)
+    const int nitem = K * half + K;
+    auto item = [&](int it, int& t, int& col) {
+        if (it < K * half) {
+            t = it >> (logN - 1);
+            col = it & (half - 1);
+        } else {
+            t = it - K * half;
+            col = half;
+        }
+    };
+    const int Q = P < 2 * K ? P : 2 * K;          // parts summed here
+    const int nrows = P > 2 * K ? tk.k0 : 0;      // partial-sum rows (parts >= 2K)
+    const int nbuf = 2 * K;                       // partial-sum buffers per row
+    const long long io_step = c - rs.io.step0;
+    c -= tk.origin;
+    const long long b = c;                        // level-0 block of the first base block
+    const int sold0 = (int)imod(b - (Q - 1), P);  // ring slot of the oldest spectrum read
+    const int snew0 = (int)imod(b, P);            // ring slot of block b
+    const float scale = tk.scale;
+    float2* sb = smem;                                   // K N: transform data
+    float2* sc = sb + (size_t)K * N;                     // K N: transform scratch
+    float2* twt = sc + (size_t)K * N;                    // N/2 quarter-wave twiddles
+    float2* hs = twt + half;                             // Q rows: H_0 .. H_{Q-1}
+    float2* xs = hs + (size_t)Q * cs;                    // Q - 1 + K rows: row i holds block b - (Q - 1) + i
+    float2* ys = xs + (size_t)(Q - 1 + K) * cs;          // K rows: Y of blocks b .. b + K - 1
+    float* emit = reinterpret_cast<float*>(ys + (size_t)K * cs);   // K N0: other levels' due slices
+    const Twiddles tw{twt, logN};
+    const bool early = io_step >= 1;   // block c - 1 lies in this call's input too
+    const int qpb = N >> 2;            // quads per base block
+    const int nqw = (K + 1) * qpb;     // window: blocks c - 1 .. c + K - 1
+    const long long isamp = rs.io.in_sample;
+    const float* in0 = rs.io.in + (long long)tk.in_ch * rs.io.in_ch;
+    auto X4 = [&](int row, int col) { return *reinterpret_cast<const float4*>(xs + (size_t)row * cs + 2 * col); };
+    auto H4 = [&](int p, int col) { return *reinterpret_cast<const float4*>(hs + (size_t)p * cs + 2 * col); };
+    // quad qd of window block bi (block c + bi - 1): second half of sub-block
+    // bi - 1's window, first half of sub-block bi's
+    auto place = [&](int qd, float4 v) {
+        const int bi = qd >> (logN - 2), w = qd & (qpb - 1);
+        if (bi < K) {
+            sb[bi * N + 2 * w] = make_float2(v.x, v.y);
+            sb[bi * N + 2 * w + 1] = make_float2(v.z, v.w);
+        }
+        if (bi >= 1) {
+            sb[(bi - 1) * N + half + 2 * w] = make_float2(v.x, v.y);
+            sb[(bi - 1) * N + half + 2 * w + 1] = make_float2(v.z, v.w);
+        }
+    };
+    // rows [r0, r0 + n) of a ring starting at slot s0 (wrapping at P): two
+    // contiguous runs; f(ring_row, first_local_row, rows)
+    auto ring_runs = [&](int s0, int n, auto&& f) {
+        const int n1 = min(n, P - s0);
+        f(s0, 0, n1);
+        if (n > n1) f(0, n1, n - n1);
+    };
+
+    // ---- static prologue: the call's input, twiddles, filter rows -----------------
+    float4 wv[MAXW];
+#pragma unroll
+    for (int i = 0; i < MAXW; ++i) {
+        const int qd = tid + i * NT;
+        const int bi = qd >> (logN - 2);
+        if (qd < nqw && (bi >= 1 || early)) {
+            const float* src = in0 + (io_step + bi - 1) * rs.io.in_step + 4LL * (qd & (qpb - 1)) * isamp;
+            wv[i] = make_float4(src[0] * scale, src[isamp] * scale, src[2 * isamp] * scale, src[3 * isamp] * scale);
+        }
+    }
+    {
+        const int sh = bank.wlog - (logN + 1);
+        for (int m = tid; m < half; m += NT) {
+            const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(twt + m));
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(bank.W + ((size_t)m << sh))
+                         : "memory");
+        }
+        const float4* H4g = reinterpret_cast<const float4*>(tk.H);
+        float4* hs4 = reinterpret_cast<float4*>(hs);
+        for (int i = tid; i < Q * ncol; i += NT) cp_async16(hs4 + i, H4g + i);   // rows 0 .. Q-1 are contiguous
+    }
+#pragma unroll
+    for (int i = 0; i < MAXW; ++i) {
+        const int qd = tid + i * NT;
+        if (qd < nqw && (qd >= qpb || early)) place(qd, wv[i]);
+    }
+    if (!early) {   // the call's first step: block c - 1 from the input ring
+        cudaGridDependencySynchronize();
+        if (tid < qpb) {
+            const long long ta = (c - 1) * (long long)N + 4LL * tid;
+            place(tid, __ldcg(reinterpret_cast<const float4*>(tk.xring + (ta & tk.rin_mask))));
+        }
+    }
+    cp_async_wait_all();
+
+    // ---- K forward transforms, X_{b+t} -> xs, X_{b+t} H_0 + ... + X_b H_t -> acc ------
+    float4 acc[MAXI];
+    {
+        __syncthreads();
+        const float2* r = fft_smem_batch<NT, MAXBB>(sb, sc, K, N, logN, tw, false);
+        for (int it = tid; it < nitem; it += NT) {
+            int t, k;
+            item(it, t, k);
+            const float2* z = r + t * N;
+            const int nk = (k == 0) ? 0 : N - k;
+            float2 xk, xnk;
+            rfft_split(z[k], z[nk], k, logN, tw, xk, xnk);
+            float2* X = xs + (size_t)(Q - 1 + t) * cs;
+            X[k] = xk;
+            if (N - k != k) X[N - k] = xnk;
+            if (k == 0) X[N + 1] = make_float2(0.f, 0.f);   // row padding
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < MAXI; ++i) {
+            const int it = tid + i * NT;
+            acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (it < nitem) {
+                int t, col;
+                item(it, t, col);
+                for (int p = 0; p <= t && p < Q; ++p) acc[i] = f4mac(acc[i], X4(Q - 1 + t - p, col), H4(p, col));
+            }
+        }
+    }
+    if (early) cudaGridDependencySynchronize();
+
+    // ---- dependent inputs: older spectra, partial sums, due output slices ---------
+    ring_runs(sold0, Q - 1, [&](int s0, int r0, int n) {
+        const float4* src = reinterpret_cast<const float4*>(tk.X + (size_t)s0 * cs);
+        float4* dst = reinterpret_cast<float4*>(xs + (size_t)r0 * cs);
+        for (int i = tid; i < n * ncol; i += NT) cp_async16(dst + i, src + i);
+    });
+    float4 ya[MAXI];
+#pragma unroll
+    for (int i = 0; i < MAXI; ++i) {
+        const int it = tid + i * NT;
+        if (nrows > 0 && it < nitem) {
+            int t, col;
+            item(it, t, col);
+            const float4* y4 = reinterpret_cast<const float4*>(tk.Yp + (size_t)((b + t) & (nbuf - 1)) * cs + 2 * col);
+            const size_t rstep = (size_t)nbuf * cs / 2;   // float4 per row
+            ya[i] = __ldcg(y4);
+            for (int q = 1; q < nrows; ++q) ya[i] = f4add(ya[i], __ldcg(y4 + q * rstep));
+        }
+    }
+    const int Le = tk.M - 1 < kEmitLevels ? tk.M - 1 : kEmitLevels;
+    const long long t_new = c * (long long)N;
+    const int nq_out = (K * N) >> 2;
+    {
+        float4 ev[MAXE][kEmitLevels];
+#pragma unroll
+        for (int i = 0; i < MAXE; ++i) {
+            const int e4 = tid + i * NT;
+#pragma unroll
+            for (int L = 0; L < kEmitLevels; ++L)
+                if (L < Le && e4 < nq_out)
+                    ev[i][L] = __ldcg(reinterpret_cast<const float4*>(tk.eyring[L] + ((t_new + 4 * e4) & tk.emask[L])));
+        }
+#pragma unroll
+        for (int i = 0; i < MAXE; ++i) {
+            const int e4 = tid + i * NT;
+            if (e4 >= nq_out || tk.M < 2) continue;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int L = 0; L < kEmitLevels; ++L)
+                if (L < Le) v = f4add(v, ev[i][L]);
+            for (int L = kEmitLevels + 1; L < tk.M; ++L) {   // rare: more than 5 levels
+                const DevLevel& l2 = bank.lv[tk.lv_index + L];
+                v = f4add(v, __ldcg(reinterpret_cast<const float4*>(l2.yring + ((t_new + 4 * e4) & l2.rmask))));
+            }
+            *reinterpret_cast<float4*>(emit + 4 * e4) = v;
+        }
+    }
+    // this step's input appended to the PC's ring (blocks c .. c + K - 1)
+#pragma unroll
+    for (int i = 0; i < MAXW; ++i) {
+        const int qd = tid + i * NT;
+        const int bi = qd >> (logN - 2);
+        if (qd < nqw && bi >= 1) {
+            const long long ta = (c + bi - 1) * (long long)N + 4LL * (qd & (qpb - 1));
+            *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();   // every thread's older-spectra copies have landed
+    // the new spectra into the ring only now: a slot read above may be one of
+    // them.  With fewer parts than blocks (one-level PCs) only the newest P
+    // blocks keep a slot.
+    {
+        const int t_keep = K > P ? K - P : 0;
+        int s0 = snew0 + t_keep;
+        if (s0 >= P) s0 -= P;
+        ring_runs(s0, K - t_keep, [&](int sr, int r0, int n) {
+            float4* dst = reinterpret_cast<float4*>(tk.X + (size_t)sr * cs);
+            const float4* src = reinterpret_cast<const float4*>(xs + (size_t)(Q - 1 + t_keep + r0) * cs);
+            for (int i = tid; i < n * ncol; i += NT) dst[i] = src[i];
+        });
+    }
+#pragma unroll
+    for (int i = 0; i < MAXI; ++i) {
+        const int it = tid + i * NT;
+        if (it < nitem) {
+            int t, col;
+            item(it, t, col);
+            float4 a = acc[i];
+            for (int p = t + 1; p < Q; ++p) a = f4mac(a, X4(Q - 1 + t - p, col), H4(p, col));
+            if (nrows > 0) a = f4add(a, ya[i]);
+            *reinterpret_cast<float4*>(ys + (size_t)t * cs + 2 * col) = a;
+        }
+    }
+    __syncthreads();
+    for (int it = tid; it < nitem; it += NT) {   // inverse pre-pass into sb
+        int t, k;
+        item(it, t, k);
+        const float2* Y = ys + (size_t)t * cs;
+        float2 zk, znk;
+        irfft_merge(Y[k], Y[N - k], k, logN, tw, zk, znk);
+        float2* s = sb + t * N;
+        s[k] = zk;
+        if (k != 0 && k != half) s[N - k] = znk;
+    }
+    __syncthreads();
+    const float* yo = reinterpret_cast<const float*>(fft_smem_batch<NT, MAXBB>(sb, sc, K, N, logN, tw, true));
+
+    // ---- output: K base blocks, each the first N samples of its inverse --------------
+    float* out = rs.io.out + io_step * rs.io.out_step;
+    const long long osamp = rs.io.out_sample, och = rs.io.out_ch;
+    const int KN = K * N;
+    for (int i = tid; i < KN; i += NT) {
+        const int t = i >> logN, j = i & (N - 1);
+        float v = yo[(size_t)t * 2 * N + j];
+        if (tk.M > 1) v += emit[i];
+        const long long o = t * rs.io.out_step + j * osamp;
+        if (tk.mix_mode == 1) out[o + (long long)tk.out_ch * och] = v;
+        else if (tk.mix_mode == 2) tk.pcout[i] = v;
+        for (int z = 0; z < tk.zero_outs; ++z) out[o + (long long)bank.zero_list[tk.zero_off + z] * och] = 0.0f;
+    }
+    if (tk.mix_mode != 2) return;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        const int o = tk.out_ch;
+        const int cnt = bank.out_off[o + 1] - bank.out_off[o];
+        *s_last = (atomicAdd(&bank.mix_cnt[o], 1) == cnt - 1);
+    }
+    __syncthreads();
+    if (!*s_last) return;
+    __threadfence();
+    const int o = tk.out_ch;
+    const int j0 = bank.out_off[o], j1 = bank.out_off[o + 1];
+    for (int i = tid; i < KN; i += NT) {
+        const int t = i >> logN, j = i & (N - 1);
+        float v = 0.0f;
+        for (int jj = j0; jj < j1; ++jj) v += __ldcg(&bank.pcs[bank.out_pcs[jj]].pcout[i]);
+        out[t * rs.io.out_step + j * osamp + (long long)o * och] = v;
+    }
+    if (tid == 0) bank.mix_cnt[o] = 0;
+}
+
 // ---------------------------------------------------------------------------
 // The step kernel: CTA i runs task i of this step's task list.
 // ---------------------------------------------------------------------------
-template <class C>
+// MULTI: the bank runs several base blocks per step (level-0 fires take
+// fire_multi); a separate instance so the one-block kernel keeps its registers.
+template <class C, bool MULTI = false>
 __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __restrict__ tasks, RunState rs_val,
                                                      const RunState* rs_dev, int step_in_batch) {
     extern __shared__ float4 dyn_smem[];
@@ -576,10 +962,24 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
     if (!rs_dev && tid == 64) rs = rs_val;
     __syncthreads();
     const long long c = rs.step_base + step_in_batch;
+    const int kb = MULTI ? bank.kb : 1;
     if (tk.kind == 1) {
         cudaGridDependencySynchronize();
-        spread_body<C::NT>(tk, c, dyn_smem);
+        if constexpr (MULTI) {
+            if (tk.T == 1) {   // level 0: the next step's kb blocks in one task
+                if (kb == 2) spread_multi<C::NT, 2>(tk, c, dyn_smem);
+                else spread_multi<C::NT, 4>(tk, c, dyn_smem);
+                return;
+            }
+        }
+        spread_body<C::NT>(tk, c, dyn_smem, kb);
         return;
+    }
+    if constexpr (MULTI && C::PREFETCH) {
+        if (tk.T == 1) {
+            fire_multi<C>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
+            return;
+        }
     }
     fire_body<C, true>(bank, tk, rs, c, reinterpret_cast<float2*>(dyn_smem), &s_last);
 }
@@ -641,7 +1041,7 @@ __global__ void __launch_bounds__(C::NT) pool_kernel(Bank bank, const Task* __re
         tk.out_ch = 0;   // partial-sum row 0
     }
     __syncthreads();
-    spread_body<C::NT>(tk, c, dyn_smem);
+    spread_body<C::NT>(tk, c, dyn_smem, 1);
 }
 
 cudaError_t launch_pool_class(int cls, int grid, int maxN, const Bank& bank, const Task* slots, const PoolCta* map,
@@ -693,6 +1093,28 @@ __global__ void __launch_bounds__(NT) spectra_kernel(const SpectraJob* __restric
     }
 }
 
+// Spread tasks of levels >= 1 with several base blocks per step: their own
+// launch beside the step chain (they feed only the levels' deferred fires).
+constexpr int kSideNT = 256;
+__global__ void __launch_bounds__(kSideNT) spread_kernel(const Task* __restrict__ tasks, RunState rs_val,
+                                                        const RunState* rs_dev, int step_in_batch) {
+    __shared__ float4 red[(kSideNT / kSpreadLanes - 1) * kSpreadLanes];
+    __shared__ __align__(16) Task tk;
+    __shared__ long long step_base;
+    const int tid = threadIdx.x;
+    if (tid < 12) reinterpret_cast<int4*>(&tk)[tid] = __ldg(reinterpret_cast<const int4*>(tasks + blockIdx.x) + tid);
+    if (tid == 32) step_base = rs_dev ? __ldcg(&rs_dev->step_base) : rs_val.step_base;
+    __syncthreads();
+    spread_body<kSideNT>(tk, step_base + step_in_batch, red, 1);
+}
+
+cudaError_t launch_side_spreads(int grid, const Task* tasks, const RunState& rs, const RunState* rs_dev,
+                                int step_in_batch, cudaStream_t st) {
+    if (grid <= 0) return cudaSuccess;
+    spread_kernel<<<grid, kSideNT, 0, st>>>(tasks, rs, rs_dev, step_in_batch);
+    return cudaGetLastError();
+}
+
 __global__ void set_state_kernel(RunState* dst, RunState v) { *dst = v; }
 
 // ---------------------------------------------------------------------------
@@ -712,10 +1134,28 @@ size_t class_smem_bytes(int cls, int maxN) {
     return b > red ? b : red;
 }
 
+size_t step_smem_bytes(int cls, int maxN, const Bank& bank) {
+    size_t b = class_smem_bytes(cls, maxN);
+    if (cls == 0 && bank.kb > 1) b = std::max(b, multi_smem_bytes(bank.N0, bank.kb));
+    return b;
+}
+
+int max_step_blocks(int N0) {
+    if (N0 < 16 || N0 > Cls0::MAXN) return 1;
+    int k = 1;
+    while (2 * k * N0 <= kMaxStepSamples && 2 * k <= kMaxStepBlocks) k *= 2;
+    return k;
+}
+
 cudaError_t prepare_kernels() {
     cudaError_t e;
+    size_t s0 = class_smem_bytes(0, Cls0::MAXN);
+    for (int N = 16; N <= Cls0::MAXN; N *= 2)
+        for (int k = 2; k <= max_step_blocks(N); k *= 2) s0 = std::max(s0, multi_smem_bytes(N, k));
     e = cudaFuncSetAttribute(step_kernel<Cls0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)class_smem_bytes(0, Cls0::MAXN));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(step_kernel<Cls0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s0);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(step_kernel<Cls1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max(class_smem_bytes(1, Cls1::MAXN), kWholeSmSmem));
@@ -764,13 +1204,15 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kNT[cls]);
-    cfg.dynamicSmemBytes = class_smem_bytes(cls, maxN);
+    cfg.dynamicSmemBytes = step_smem_bytes(cls, maxN, bank);
     if (whole_sm && cls != 0) cfg.dynamicSmemBytes = std::max(cfg.dynamicSmemBytes, kWholeSmSmem);
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = na;
     switch (cls) {
-        case 0: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
+        case 0:
+            if (bank.kb > 1) return cudaLaunchKernelEx(&cfg, step_kernel<Cls0, true>, bank, tasks, rs, rs_dev, step_in_batch);
+            return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
         case 1: return cudaLaunchKernelEx(&cfg, step_kernel<Cls1>, bank, tasks, rs, rs_dev, step_in_batch);
         default: return cudaLaunchKernelEx(&cfg, step_kernel<Cls2>, bank, tasks, rs, rs_dev, step_in_batch);
     }

@@ -54,12 +54,17 @@ def _i32(a) -> np.ndarray:
 class PartConvMulti:
     relaxed = 0
 
-    def __init__(self, verbosity: int = 0):
+    def __init__(self, verbosity: int = 0, step_blocks: int = 1):
+        """step_blocks > 1: offline throughput mode, `step_blocks` base blocks
+        per step (pc_set_step_blocks); run() is then unavailable and process()
+        wants a multiple of step_blocks * buffer_size frames."""
         self.verbosity = verbosity
         self._lib = nat.lib()
         self._h = self._lib.pc_create(int(verbosity))
         if not self._h:
             raise PartConvError(nat.PC_ERR_NOMEM, "pc_create failed")
+        if step_blocks != 1:
+            nat.check(self._h, self._lib.pc_set_step_blocks(self._h, int(step_blocks)))
         self.FS = 0
         self.buffer_size = 0
         self.max_block_size = 0
@@ -112,6 +117,7 @@ class PartConvMulti:
         self.max_block_size = info.max_block_size
         self.numInputChannels = info.num_input_channels
         self.numOutputChannels = info.num_output_channels
+        self.step_blocks = info.step_blocks
         self.output_mix = np.zeros(self.buffer_size * self.numOutputChannels, np.float32)
         self.input_mix = np.zeros(self.buffer_size * self.numInputChannels, np.float32)
         self._frame_num = 0

@@ -100,6 +100,18 @@ def test_calls_before_setup_return_errors():
     lib.pc_destroy(h)
 
 
+def test_step_blocks_argument_checks():
+    lib = nat.lib()
+    h = lib.pc_create(0)
+    for k in (1, 2, 4, 8):
+        assert lib.pc_set_step_blocks(h, k) == nat.PC_OK
+    for k in (0, 3, 16, -1):
+        assert lib.pc_set_step_blocks(h, k) == nat.PC_ERR_ARG
+    assert b"step blocks" in lib.pc_last_error(h)
+    assert lib.pc_set_step_blocks(None, 2) == nat.PC_ERR_ARG
+    lib.pc_destroy(h)
+
+
 def test_setup_config_errors_without_exiting(tmp_path):
     lib = nat.lib()
     h = lib.pc_create(0)

@@ -439,6 +439,8 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             while (KB > 1 && (p.N[L] / N0) % KB) KB >>= 1;
     h->KB = KB;
     h->Hs = std::max(1, Hh / KB);
+    // parts a K-block level-0 fire sums itself; spread rows take the rest
+    const int QC = KB > 1 ? multi_fire_parts(N0, KB) : 2;
     h->G = std::max(h->G, KB);
 
     // ---- arena layout --------------------------------------------------------------
@@ -564,7 +566,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 l.rmask = rl[li] - 1;
                 l.pc = i;
                 {   // spread tasks sum parts >= 2 KB (level 0), >= 2 (deferred levels) or >= 1
-                    const int p_lo = L == 0 ? 2 * KB : (dfl[li] ? 2 : 1);
+                    const int p_lo = L == 0 ? (KB > 1 ? std::min(p.P[L], QC) : 2) : (dfl[li] ? 2 : 1);
                     const int np = p.P[L] - p_lo;
                     l.npart = np > 0 ? (np + spread_task_parts() - 1) / spread_task_parts() : 1;
                 }
@@ -719,9 +721,10 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             const int cls = fire_class_of(l.N);
             if (l.T == 1) {   // level 0: KB blocks, parts < 2 KB in the fire
                 Task t = fire_task(li);
-                const int Q = std::min(l.P, 2 * KB);
-                const int rows = l.P > 2 * KB ? l.npart : 0;
+                const int Q = std::min(l.P, QC);
+                const int rows = l.P > Q ? l.npart : 0;
                 t.k0 = rows;
+                t.p_lo = Q;
                 // per block: H_0 read and the new X row written, Q - 1 older
                 // (H, X) row pairs, the partial-sum rows, 2N window samples read
                 // and N written, the other levels' due slices, the ring append
@@ -769,9 +772,9 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                     }
                 bytes += blocks * (16.0 * (l.P - p_lo) + 8.0 * l.npart) * (hi - lo);
             };
-            if (l.T == 1) {   // parts >= 2 KB of the next step's blocks S KB + KB .. S KB + 2 KB - 1
-                if (l.P <= 2 * KB) continue;
-                add_spreads(0, l.cs, 2 * KB, -(long long)(KB - 1), lists[sc][g], h->alg_bytes[sc][g], KB);
+            if (l.T == 1) {   // parts >= Q of the next step's blocks S KB + KB .. S KB + 2 KB - 1
+                if (l.P <= QC) continue;
+                add_spreads(0, l.cs, QC, -(long long)(KB - 1), lists[sc][g], h->alg_bytes[sc][g], KB);
                 continue;
             }
             if (l.P < 3) continue;
@@ -950,6 +953,8 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->bank.wlog = kWlog;
     h->bank.N0 = N0;
     h->bank.kb = KB;
+    h->bank.kq = 0;
+    for (auto& p : h->specs) h->bank.kq = std::max(h->bank.kq, std::min(p.P[0], QC));
     h->bank.n_out = n_out;
     h->bank.out_off = reinterpret_cast<const int*>(A + off_out_off);
     h->bank.out_pcs = reinterpret_cast<const int*>(A + off_out_pcs);

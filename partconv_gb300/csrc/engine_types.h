@@ -67,6 +67,7 @@ struct Task {
     int k0, k1, M, in_ch;
     int out_ch, mix_mode, zero_outs, zero_off;
     int rin_mask, lv_index, p_lo, active;   // p_lo: first part summed by a spread task
+                                            // (K-block level-0 fire: the parts it sums itself)
     float scale;
     int dfer;           // 1: the level's fire runs off the step chain (deferred), see engine.cu
     // step at which this PC's time starts (serving pools); in a static bank
@@ -117,6 +118,7 @@ struct Bank {
     int N0;
     int n_out;
     int kb;                // base blocks per step (level-0 sub-blocks of one fire); 0 or 1: one
+    int kq;                // with kb > 1: most parts a level-0 fire sums itself (shared-memory size)
     // per output channel mixing lists (mix_mode 2): out_off[o]..out_off[o+1]
     const int* out_off;
     const int* out_pcs;

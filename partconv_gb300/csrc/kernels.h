@@ -32,6 +32,9 @@ size_t step_smem_bytes(int cls, int maxN, const Bank& bank);
 // largest base-blocks-per-step K (a power of two <= 4) the level-0 kernel
 // supports for base block N0 (K N0 <= 1024); 1 if none
 int max_step_blocks(int N0);
+// parts a K-block level-0 fire sums itself (the rest come from spread rows):
+// the most that keep two of its CTAs per SM, at least 2K
+int multi_fire_parts(int N0, int K);
 
 cudaError_t prepare_kernels();
 // pdl: let the launch overlap the previous kernel in the stream, which must

@@ -649,10 +649,11 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Level 0 over K base blocks per step (bank.kb = K > 1; offline processing
 // of many blocks per call): the CTA of one PC computes its blocks
 // b = c .. c + K - 1.  Block b + t sums X_{b+t-p} H_p over the parts
-// p < Q = min(P, 2K) here -- p <= t from this CTA's own forward transforms,
-// the others from the spectra ring -- and adds the partial-sum rows of the
-// parts p >= 2K that spread tasks built during the previous step (those read
-// only spectra of blocks <= b - 1).  Order: p ascending, then the rows in
+// p < Q here (Q = min(P, the shared-memory cap) >= min(P, 2K), in the task's
+// p_lo) -- p <= t from this CTA's own forward transforms, the others from
+// the spectra ring -- and adds the partial-sum rows of the parts p >= Q that
+// spread tasks built during the previous step (those read only spectra of
+// blocks <= b - 1 since Q >= 2K).  Order: p ascending, then the rows in
 // order.  The K forward and K inverse transforms run as one batched
 // shared-memory FFT: a 256-point transform has 64 radix-4 butterflies per
 // stage, so four of them fill a 256-thread CTA for the cost of one.
@@ -662,11 +663,16 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 constexpr int kMaxStepSamples = 1024;   // K N0 at most
 constexpr int kMaxStepBlocks = 4;       // K at most
 
-__host__ __device__ constexpr size_t multi_smem_bytes(int N, int K) {
-    // transform buffers 2 K N, twiddles N/2 (complex); filter rows 2K, spectra
-    // rows 3K - 1, sums K (rows of N + 2 complex); due output slices K N floats
-    return (size_t)8 * (2 * (size_t)K * N + (size_t)N / 2 + (size_t)(6 * K - 1) * (N + 2)) + (size_t)4 * K * N;
+// shared memory of fire_multi summing Q parts itself
+__host__ __device__ constexpr size_t multi_smem_bytes(int N, int K, int Q) {
+    // transform buffers 2 K N, twiddles N/2 (complex); filter rows Q, spectra
+    // rows Q - 1 + K, sums K (rows of N + 2 complex); due output slices K N floats
+    return (size_t)8 * (2 * (size_t)K * N + (size_t)N / 2 + (size_t)(2 * Q + 2 * K - 1) * (N + 2)) +
+           (size_t)4 * K * N;
 }
+// shared memory that still lets two such CTAs share an SM
+constexpr size_t kMultiSmemCap = 112 * 1024;
+constexpr int kMaxMultiParts = 32;
 
 template <class C>
 __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, const RunState& rs, long long c,
@@ -692,8 +698,8 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
             col = half;
         }
     };
-    const int Q = P < 2 * K ? P : 2 * K;          // parts summed here
-    const int nrows = P > 2 * K ? tk.k0 : 0;      // partial-sum rows (parts >= 2K)
+    const int Q = tk.p_lo;                        // parts summed here: min(P, cap), >= min(P, 2K)
+    const int nrows = P > Q ? tk.k0 : 0;          // partial-sum rows (parts >= Q)
     const int nbuf = 2 * K;                       // partial-sum buffers per row
     const long long io_step = c - rs.io.step0;
     c -= tk.origin;
@@ -1136,8 +1142,14 @@ size_t class_smem_bytes(int cls, int maxN) {
 
 size_t step_smem_bytes(int cls, int maxN, const Bank& bank) {
     size_t b = class_smem_bytes(cls, maxN);
-    if (cls == 0 && bank.kb > 1) b = std::max(b, multi_smem_bytes(bank.N0, bank.kb));
+    if (cls == 0 && bank.kb > 1) b = std::max(b, multi_smem_bytes(bank.N0, bank.kb, bank.kq));
     return b;
+}
+
+int multi_fire_parts(int N0, int K) {
+    int q = 2 * K;
+    while (q < kMaxMultiParts && multi_smem_bytes(N0, K, q + 1) <= kMultiSmemCap) ++q;
+    return q;
 }
 
 int max_step_blocks(int N0) {
@@ -1151,7 +1163,7 @@ cudaError_t prepare_kernels() {
     cudaError_t e;
     size_t s0 = class_smem_bytes(0, Cls0::MAXN);
     for (int N = 16; N <= Cls0::MAXN; N *= 2)
-        for (int k = 2; k <= max_step_blocks(N); k *= 2) s0 = std::max(s0, multi_smem_bytes(N, k));
+        for (int k = 2; k <= max_step_blocks(N); k *= 2) s0 = std::max(s0, multi_smem_bytes(N, k, multi_fire_parts(N, k)));
     e = cudaFuncSetAttribute(step_kernel<Cls0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)class_smem_bytes(0, Cls0::MAXN));
     if (e != cudaSuccess) return e;

@@ -44,8 +44,8 @@ using namespace pcg;
 namespace {
 
 constexpr int kWlog = 15;
-constexpr int kMacNT = 128;        // MAC CTA: 2 groups x 64 lanes, two bins per lane
-constexpr int kMacLanes = 64;
+constexpr int kMacNT = 128;        // MAC CTA: 4 groups x 32 lanes, two bins per lane
+constexpr int kMacLanes = 32;
 constexpr int kMacBins = 2 * kMacLanes;
 constexpr int kMaxMimoLevels = 8;
 constexpr int kMaxMacTerms = 2048;  // (input, part) terms one MAC task sums

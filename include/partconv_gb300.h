@@ -350,6 +350,14 @@ pcs_handle* pcs_create(int buffer_size, long long hbm_budget_bytes, int max_pcs)
 /* Admit one PC (IR, layout as pc_check_layout, at most 5 levels); its id is
  * also its I/O channel.  Its schedule starts at the pool's next step. */
 int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, int* P, int* pc_id);
+/* Same without waiting for the PC's spectra: the PC is pending until a
+ * pcs_poll finds its admission work completed and makes it live (its
+ * schedule then starts at the pool's next step; pcs_is_live tells). */
+int pcs_admit_async(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, int* P, int* pc_id);
+/* Make live every pending PC whose admission work has completed; the count
+ * goes to *n_published (may be NULL). */
+int pcs_poll(pcs_handle* h, int* n_published);
+int pcs_is_live(const pcs_handle* h, int pc_id);
 int pcs_release(pcs_handle* h, int pc_id);
 /* One step: host in/out [n_channels][buffer_size] (pinned for asynchrony);
  * returns after enqueueing; pcs_query / pcs_sync observe completion. */

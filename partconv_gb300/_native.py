@@ -125,6 +125,9 @@ SIGNATURES = {
     "pcd_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "pcs_create": (C.c_void_p, [C.c_int, C.c_longlong, C.c_int]),
     "pcs_admit": (C.c_int, [C.c_void_p, _f32p, C.c_int, C.c_int, _i32p, _i32p, C.POINTER(C.c_int)]),
+    "pcs_admit_async": (C.c_int, [C.c_void_p, _f32p, C.c_int, C.c_int, _i32p, _i32p, C.POINTER(C.c_int)]),
+    "pcs_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "pcs_is_live": (C.c_int, [C.c_void_p, C.c_int]),
     "pcs_release": (C.c_int, [C.c_void_p, C.c_int]),
     "pcs_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "pcs_query": (C.c_int, [C.c_void_p]),

@@ -77,6 +77,12 @@ struct FreeList {
 
 struct PoolPC {
     bool live = false;
+    // admitted, spectra still being built on the admission stream: becomes
+    // live in pcs_poll once `ev` has completed
+    bool pending = false;
+    cudaEvent_t ev = nullptr;
+    size_t toff = 0, tbytes = 0;  // IR and job scratch of the admission
+    std::vector<Task> recs;       // descriptors to publish
     int M = 0;
     std::vector<int> N, P;
     size_t off = 0, bytes = 0;   // arena block
@@ -108,6 +114,7 @@ struct pcs_handle {
     int class_maxN[3] = {0, 0, 0};
     std::vector<PoolPC> pcs;
     int live = 0;
+    std::vector<int> pending;   // ids of admitted PCs not yet live
     long long launches = 0;
     cudaEvent_t done = nullptr;
     std::vector<void*> allocs;
@@ -267,9 +274,11 @@ pcs_handle* pcs_create(int buffer_size, long long hbm_budget_bytes, int max_pcs)
     return h;
 }
 
-// Admit one PC (one stream channel): returns its id (also its I/O channel)
-// in *pc_id.  PC_ERR_NOMEM when the pool's HBM budget cannot hold it now.
-int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, int* P, int* pc_id) {
+// Admit one PC (one stream channel) without waiting: its state is cleared
+// and its spectra built on the admission stream; pcs_poll makes it live once
+// that work has completed.  Returns its id (also its I/O channel) in *pc_id.
+// PC_ERR_NOMEM when the pool's HBM budget cannot hold it now.
+int pcs_admit_async(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, int* P, int* pc_id) {
     if (!h) return PC_ERR_ARG;
     if (!ir || ir_len < 1 || !N || !P || !pc_id) return sfail(h, PC_ERR_ARG, "bad admission arguments");
     if (M > kPoolMaxLevels) return sfail(h, PC_ERR_LIMIT, "at most 5 levels per pooled PC");
@@ -281,7 +290,7 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
     for (int i = 0; i < M; ++i) P[i] = Pv[i];
     int id = -1;
     for (int i = 0; i < h->max_pcs; ++i)
-        if (!h->pcs[i].live) {
+        if (!h->pcs[i].live && !h->pcs[i].pending) {
             id = i;
             break;
         }
@@ -370,7 +379,7 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
         t.lv_index = 0;
         t.active = 1;
         t.scale = 1.0f;
-        t.origin = h->step;
+        t.origin = 0;   // set when the PC goes live
         t.H = H;
         t.X = X;
         t.Yp = Yp;
@@ -400,27 +409,94 @@ int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, i
         h->launches++;
         jo += jobs[c].size();
     }
-    for (int L = 0; L < M; ++L) {
-        h->h_slots[(size_t)id * kPoolMaxLevels + L] = recs[L];
-        h->class_maxN[fire_class_of(Nv[L])] = std::max(h->class_maxN[fire_class_of(Nv[L])], Nv[L]);
-    }
-    h->class_maxN[fire_class_of(h->N0)] = std::max(h->class_maxN[fire_class_of(h->N0)], h->N0);
-    // the PC's state and spectra are ready before its descriptors reach the
-    // pool's stream (waiting only for the admission work, not for steps)
-    SCK(cudaStreamSynchronize(h->astream), "admission sync");
-    h->fl.release(toff, ir_bytes + job_bytes);
-    SCK(cudaMemcpyAsync(h->d_slots + (size_t)id * kPoolMaxLevels, recs.data(), sizeof(Task) * M, cudaMemcpyHostToDevice,
-                        h->stream),
-        "descriptor upload");
-    pc.live = true;
-    h->live++;
+    // the PC's state and spectra must be ready before its descriptors reach
+    // the pool's stream: the admission work is marked by an event
+    SCK(cudaEventCreateWithFlags(&pc.ev, cudaEventDisableTiming), "event");
+    SCK(cudaEventRecord(pc.ev, h->astream), "event record");
+    pc.toff = toff;
+    pc.tbytes = ir_bytes + job_bytes;
+    pc.recs = std::move(recs);
+    pc.pending = true;
+    h->pending.push_back(id);
     *pc_id = id;
-    return rebuild_map(h);
+    return PC_OK;
+}
+
+// Publish every pending PC whose admission work has completed (all of them
+// when wait): descriptors to the pool's stream, time origin = the next step.
+static int pcs_poll_impl(pcs_handle* h, bool wait, int* n_published) {
+    int n = 0;
+    for (size_t j = 0; j < h->pending.size();) {
+        const int id = h->pending[j];
+        PoolPC& pc = h->pcs[id];
+        if (wait) SCK(cudaEventSynchronize(pc.ev), "admission sync");
+        const cudaError_t q = cudaEventQuery(pc.ev);
+        if (q == cudaErrorNotReady) {
+            ++j;
+            continue;
+        }
+        if (q != cudaSuccess) return sfail(h, PC_ERR_CUDA, std::string("admission: ") + cudaGetErrorString(q));
+        cudaEventDestroy(pc.ev);
+        pc.ev = nullptr;
+        h->fl.release(pc.toff, pc.tbytes);
+        for (auto& t : pc.recs) t.origin = h->step;
+        for (int L = 0; L < pc.M; ++L) {
+            h->h_slots[(size_t)id * kPoolMaxLevels + L] = pc.recs[L];
+            const int cls = fire_class_of(pc.N[L]);
+            h->class_maxN[cls] = std::max(h->class_maxN[cls], pc.N[L]);
+        }
+        h->class_maxN[fire_class_of(h->N0)] = std::max(h->class_maxN[fire_class_of(h->N0)], h->N0);
+        SCK(cudaMemcpyAsync(h->d_slots + (size_t)id * kPoolMaxLevels, pc.recs.data(), sizeof(Task) * pc.M,
+                            cudaMemcpyHostToDevice, h->stream),
+            "descriptor upload");
+        // pageable source: staged before the call returns, so pc.recs may change later
+        pc.pending = false;
+        pc.live = true;
+        h->live++;
+        ++n;
+        h->pending.erase(h->pending.begin() + j);
+    }
+    if (n_published) *n_published = n;
+    return n ? rebuild_map(h) : PC_OK;
+}
+
+// Admit one PC and make it live before returning (its schedule starts at
+// the pool's next step).
+int pcs_admit(pcs_handle* h, const float* ir, int ir_len, int M, const int* N, int* P, int* pc_id) {
+    int r = pcs_admit_async(h, ir, ir_len, M, N, P, pc_id);
+    if (r) return r;
+    return pcs_poll_impl(h, true, nullptr);
+}
+
+int pcs_poll(pcs_handle* h, int* n_published) {
+    if (!h) return PC_ERR_ARG;
+    if (h->pending.empty()) {
+        if (n_published) *n_published = 0;
+        return PC_OK;
+    }
+    SCK(cudaSetDevice(h->device), "cudaSetDevice");
+    return pcs_poll_impl(h, false, n_published);
+}
+
+int pcs_is_live(const pcs_handle* h, int pc_id) {
+    if (!h || pc_id < 0 || pc_id >= h->max_pcs) return 0;
+    return h->pcs[pc_id].live ? 1 : 0;
 }
 
 int pcs_release(pcs_handle* h, int pc_id) {
-    if (!h || pc_id < 0 || pc_id >= h->max_pcs || !h->pcs[pc_id].live) return h ? sfail(h, PC_ERR_ARG, "no such PC") : PC_ERR_ARG;
+    if (!h || pc_id < 0 || pc_id >= h->max_pcs || !(h->pcs[pc_id].live || h->pcs[pc_id].pending))
+        return h ? sfail(h, PC_ERR_ARG, "no such PC") : PC_ERR_ARG;
     PoolPC& pc = h->pcs[pc_id];
+    if (pc.pending) {   // never stepped: its space is free once the admission work has run
+        SCK(cudaEventSynchronize(pc.ev), "admission sync");
+        cudaEventDestroy(pc.ev);
+        pc.ev = nullptr;
+        h->fl.release(pc.toff, pc.tbytes);
+        h->fl.release(pc.off, pc.bytes);
+        pc.pending = false;
+        h->pending.erase(std::find(h->pending.begin(), h->pending.end(), pc_id));
+        return PC_OK;
+    }
     std::vector<Task> recs(pc.M, Task{});   // inactive descriptors
     SCK(cudaMemcpyAsync(h->d_slots + (size_t)pc_id * kPoolMaxLevels, recs.data(), sizeof(Task) * pc.M,
                         cudaMemcpyHostToDevice, h->stream),
@@ -495,6 +571,9 @@ void pcs_destroy(pcs_handle* h) {
     if (!h) return;
     if (h->device >= 0) cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->astream) cudaStreamSynchronize(h->astream);
+    for (auto& pc : h->pcs)
+        if (pc.ev) cudaEventDestroy(pc.ev);
     for (auto& t : h->tmp) cudaEventDestroy(t.ev);
     h->tmp.clear();
     for (void* p : h->allocs) cudaFree(p);

@@ -60,14 +60,26 @@ class ServingPool:
         if code != nat.PC_OK:
             raise PartConvError(code, self._lib.pcs_last_error(self._h).decode())
 
-    def admit(self, ir, N, P) -> int:
+    def admit(self, ir, N, P, wait: bool = True) -> int:
+        """Admit one channel.  wait=False returns at once with the PC pending:
+        poll() makes it live when its spectra are built (is_live tells)."""
         ir = np.ascontiguousarray(ir, dtype=np.float32)
         Nv = np.ascontiguousarray(N, dtype=np.int32)
         Pv = np.ascontiguousarray(P, dtype=np.int32).copy()
         pid = C.c_int(-1)
-        self._check(self._lib.pcs_admit(self._h, ir.ctypes.data_as(nat._f32p), len(ir), len(Nv),
-                                        Nv.ctypes.data_as(nat._i32p), Pv.ctypes.data_as(nat._i32p), C.byref(pid)))
+        fn = self._lib.pcs_admit if wait else self._lib.pcs_admit_async
+        self._check(fn(self._h, ir.ctypes.data_as(nat._f32p), len(ir), len(Nv),
+                       Nv.ctypes.data_as(nat._i32p), Pv.ctypes.data_as(nat._i32p), C.byref(pid)))
         return pid.value
+
+    def poll(self) -> int:
+        """Make live the pending PCs whose admission work has completed."""
+        n = C.c_int(0)
+        self._check(self._lib.pcs_poll(self._h, C.byref(n)))
+        return n.value
+
+    def is_live(self, pc_id: int) -> bool:
+        return self._lib.pcs_is_live(self._h, int(pc_id)) == 1
 
     def release(self, pc_id: int):
         self._check(self._lib.pcs_release(self._h, int(pc_id)))
@@ -277,6 +289,10 @@ class Server:
         st = {b: dict(pid=np.zeros(0, np.int64), off=np.zeros(0, np.int64), pos=np.zeros(0, np.int64),
                       left=np.zeros(0, np.int64), req=np.zeros(0, np.int64)) for b in pools}
         pcs_of = {}
+        waiting = []   # (request, block size, channel ids) admitted, not yet live
+        pool_lat = {b: [] for b in pools}   # per-step latency by base block size
+        pool_blocks = {b: 0 for b in pools}
+        pool_miss = {b: 0 for b in pools}
         next_tick = {b: 0.0 for b in pools}
         inflight = {b: None for b in pools}
         lat_us, lat_w, miss_w, blocks = [], [], 0, 0
@@ -298,8 +314,8 @@ class Server:
                 got = []
                 ok = True
                 for ch in range(spec["channels"]):
-                    try:
-                        got.append(pools[b].admit(irs[ri][ch], N, P))
+                    try:   # asynchronous: the spectra build while the pools keep stepping
+                        got.append(pools[b].admit(irs[ri][ch], N, P, wait=False))
                     except PartConvError as e:
                         if e.code not in (nat.PC_ERR_NOMEM, nat.PC_ERR_LIMIT):
                             raise
@@ -310,17 +326,28 @@ class Server:
                         pools[b].release(pid)
                     break
                 queue.pop(0)
-                nblk = spec["frames"] // b
+                waiting.append((ri, b, got))
+                pcs_of[ri] = got
+                concurrent += 1
+                peak = max(peak, concurrent)
+            # admitted channels whose spectra are ready join at the next tick
+            if waiting:
+                for pool in pools.values():
+                    pool.poll()
+            still = []
+            for ri, b, got in waiting:
+                if not all(pools[b].is_live(pid) for pid in got):
+                    still.append((ri, b, got))
+                    continue
+                spec = requests[ri]
                 s = st[b]
                 k = len(got)
                 s["pid"] = np.concatenate([s["pid"], np.array(got, np.int64)])
                 s["off"] = np.concatenate([s["off"], rng.integers(0, nz - spec["frames"], k)])
                 s["pos"] = np.concatenate([s["pos"], np.zeros(k, np.int64)])
-                s["left"] = np.concatenate([s["left"], np.full(k, nblk, np.int64)])
+                s["left"] = np.concatenate([s["left"], np.full(k, spec["frames"] // b, np.int64)])
                 s["req"] = np.concatenate([s["req"], np.full(k, ri, np.int64)])
-                pcs_of[ri] = got
-                concurrent += 1
-                peak = max(peak, concurrent)
+            waiting = still
             progressed = False
             for b, pool in pools.items():
                 s = st[b]
@@ -329,8 +356,11 @@ class Server:
                     lat = (time.perf_counter() - t0 - tick_t) * 1e6
                     lat_us.append(lat)
                     lat_w.append(nmem)
+                    pool_lat[b].append(lat)
+                    pool_blocks[b] += nmem
                     if lat > period[b] * 1e6:
                         miss_w += nmem
+                        pool_miss[b] += nmem
                     blocks += nmem
                     inflight[b] = None
                     progressed = True
@@ -371,4 +401,12 @@ class Server:
                 "latency_us_p50": pct(0.50), "latency_us_p99": pct(0.99),
                 "latency_us_max": float(lat.max()) if len(lat) else None,
                 "deadline_miss_rate": miss_w / max(blocks, 1),
+                "per_block_size": {str(b): {"period_us": period[b] * 1e6, "steps": len(pool_lat[b]),
+                                            "blocks": pool_blocks[b],
+                                            "step_latency_us_p50": float(np.percentile(pool_lat[b], 50))
+                                            if pool_lat[b] else None,
+                                            "step_latency_us_p99": float(np.percentile(pool_lat[b], 99))
+                                            if pool_lat[b] else None,
+                                            "deadline_miss_rate": pool_miss[b] / max(pool_blocks[b], 1)}
+                                   for b in pools},
                 "launches": sum(p.kernel_launches() for p in pools.values())}

@@ -80,3 +80,59 @@ def test_realtime_latency_accounting(gpu):
     assert stats["latency_us_p50"] > 0 and stats["latency_us_p99"] >= stats["latency_us_p50"]
     assert 0.0 <= stats["deadline_miss_rate"] <= 1.0
     print("serving latency:", {k: round(v, 1) for k, v in stats.items() if "latency" in k})
+
+
+def test_async_admission_equals_blocking(gpu):
+    """pcs_admit_async + pcs_poll: the PC goes live once its spectra are
+    built and then produces the same samples as a blocking admission; a
+    pending PC can be released and its space returns to the budget."""
+    import time
+
+    from partconv_gb300.serving import ServingPool
+
+    rng = np.random.default_rng(11)
+    N0 = 128
+    ir = wl.decaying_ir(rng, 40000, 0.5)
+    N, P = serving_layout(len(ir), N0)
+    a = ServingPool(N0, 1 << 28, 4)
+    b = ServingPool(N0, 1 << 28, 4)
+    pa = a.admit(ir, N, P)
+    pb = b.admit(ir, N, P, wait=False)
+    for _ in range(20000):
+        b.poll()
+        if b.is_live(pb):
+            break
+        time.sleep(1e-4)
+    assert a.is_live(pa) and b.is_live(pb) and pa == pb == 0
+    x = (0.1 * rng.standard_normal((60, N0))).astype(np.float32)
+    ya, yb = np.zeros_like(x), np.zeros_like(x)
+    bi = np.zeros((1, N0), np.float32)
+    bo = np.zeros((1, N0), np.float32)
+    for pool, y in ((a, ya), (b, yb)):
+        for t in range(len(x)):
+            bi[0] = x[t]
+            pool.step(bi.ctypes.data, bo.ctypes.data, 1)
+            pool.sync()
+            y[t] = bo[0]
+    assert np.array_equal(ya, yb)
+    used = b.bytes_in_use()
+    pc2 = b.admit(ir, N, P, wait=False)
+    assert not b.is_live(pc2) and b.bytes_in_use() > used
+    b.release(pc2)
+    b.poll()
+    assert not b.is_live(pc2) and b.bytes_in_use() == used
+
+
+def test_load_run_with_async_admission(gpu):
+    """The real-time load loop admits without blocking and still serves
+    every request to completion."""
+    reqs = _requests(12, 13, rate=300.0, seconds=0.2)
+    irs = []
+    for r in reqs:
+        g = np.random.Generator(np.random.PCG64(r["seed"]))
+        irs.append([wl.decaying_ir(g, r["ir_len"], r["t60"]) for _ in range(r["channels"])])
+    noise = (0.1 * np.random.default_rng(3).standard_normal(1 << 18)).astype(np.float32)
+    srv = Server(hbm_budget_bytes=1 << 29, max_pcs_per_pool=64)
+    stats = srv.run_load(reqs, irs, noise, max_concurrent=100, max_seconds=30.0)
+    assert stats["finished"] == len(reqs)
+    assert stats["blocks"] > 0 and stats["latency_us_p99"] >= stats["latency_us_p50"] > 0

@@ -328,6 +328,26 @@ __device__ __noinline__ float2* fft_smem_batch(float2* a, float2* b, int K, int 
     return a;
 }
 
+// fft_smem_batch for a compile-time size N = 2^LOGN: the stage loop unrolls
+// and every shift, mask and twiddle stride is a constant.
+template <int NT, int MAXB, int LOGN>
+__device__ __noinline__ float2* fft_smem_batch_c(float2* a, float2* b, int K, const float2* twtab, bool inv) {
+    constexpr int N = 1 << LOGN;
+    const Twiddles tw{twtab, LOGN};
+#pragma unroll
+    for (int lgNs = 0; lgNs + 2 <= LOGN; lgNs += 2) {
+        stage_r4_batch<NT, MAXB>(a, b, K, N, LOGN, 1 << lgNs, lgNs, tw, inv);
+        float2* t = a;
+        a = b;
+        b = t;
+    }
+    if (LOGN & 1) {
+        stage_r2_batch<NT, MAXB>(a, b, K, N, LOGN, 1 << (LOGN - 1), LOGN - 1, tw, inv);
+        a = b;
+    }
+    return a;
+}
+
 // Split post-pass for the pair (k, N-k), 0 <= k <= N/2, on Z = FFT_N(z).
 // Returns X[k] in xk and X[N-k] in xnk (for k == 0: X[0] and X[N]).
 template <bool SW = false>

@@ -715,6 +715,16 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
     float2* ys = xs + (size_t)(Q - 1 + K) * cs;          // K rows: Y of blocks b .. b + K - 1
     float* emit = reinterpret_cast<float*>(ys + (size_t)K * cs);   // K N0: other levels' due slices
     const Twiddles tw{twt, logN};
+    // the K transforms, unrolled for the common base blocks
+    auto fftb = [&](bool inv) -> float2* {
+        switch (logN) {
+            case 6: return fft_smem_batch_c<NT, MAXBB, 6>(sb, sc, K, twt, inv);
+            case 7: return fft_smem_batch_c<NT, MAXBB, 7>(sb, sc, K, twt, inv);
+            case 8: return fft_smem_batch_c<NT, MAXBB, 8>(sb, sc, K, twt, inv);
+            case 9: return fft_smem_batch_c<NT, MAXBB, 9>(sb, sc, K, twt, inv);
+            default: return fft_smem_batch<NT, MAXBB>(sb, sc, K, N, logN, tw, inv);
+        }
+    };
     const bool early = io_step >= 1;   // block c - 1 lies in this call's input too
     const int qpb = N >> 2;            // quads per base block
     const int nqw = (K + 1) * qpb;     // window: blocks c - 1 .. c + K - 1
@@ -783,7 +793,7 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
     float4 acc[MAXI];
     {
         __syncthreads();
-        const float2* r = fft_smem_batch<NT, MAXBB>(sb, sc, K, N, logN, tw, false);
+        const float2* r = fftb(false);
         for (int it = tid; it < nitem; it += NT) {
             int t, k;
             item(it, t, k);
@@ -882,16 +892,29 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
             for (int i = tid; i < n * ncol; i += NT) dst[i] = src[i];
         });
     }
+    // older spectra: the thread's items advance together over p (each still
+    // sums p ascending), so their shared-memory loads overlap
+    {
+        int ti[MAXI], ci[MAXI];
 #pragma unroll
-    for (int i = 0; i < MAXI; ++i) {
-        const int it = tid + i * NT;
-        if (it < nitem) {
-            int t, col;
-            item(it, t, col);
+        for (int i = 0; i < MAXI; ++i) {
+            const int it = tid + i * NT;
+            ti[i] = Q;   // no parts for an item beyond the end
+            ci[i] = 0;
+            if (it < nitem) item(it, ti[i], ci[i]);
+        }
+#pragma unroll 2
+        for (int p = 1; p < Q; ++p) {
+#pragma unroll
+            for (int i = 0; i < MAXI; ++i)
+                if (p > ti[i]) acc[i] = f4mac(acc[i], X4(Q - 1 + ti[i] - p, ci[i]), H4(p, ci[i]));
+        }
+#pragma unroll
+        for (int i = 0; i < MAXI; ++i) {
+            if (tid + i * NT >= nitem) continue;
             float4 a = acc[i];
-            for (int p = t + 1; p < Q; ++p) a = f4mac(a, X4(Q - 1 + t - p, col), H4(p, col));
             if (nrows > 0) a = f4add(a, ya[i]);
-            *reinterpret_cast<float4*>(ys + (size_t)t * cs + 2 * col) = a;
+            *reinterpret_cast<float4*>(ys + (size_t)ti[i] * cs + 2 * ci[i]) = a;
         }
     }
     __syncthreads();
@@ -906,12 +929,23 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
         if (k != 0 && k != half) s[N - k] = znk;
     }
     __syncthreads();
-    const float* yo = reinterpret_cast<const float*>(fft_smem_batch<NT, MAXBB>(sb, sc, K, N, logN, tw, true));
+    const float* yo = reinterpret_cast<const float*>(fftb(true));
 
     // ---- output: K base blocks, each the first N samples of its inverse --------------
     float* out = rs.io.out + io_step * rs.io.out_step;
     const long long osamp = rs.io.out_sample, och = rs.io.out_ch;
     const int KN = K * N;
+    float* orow = out + (long long)tk.out_ch * och;
+    if (tk.mix_mode == 1 && tk.zero_outs == 0 && osamp == 1 && (rs.io.out_step & 3) == 0 &&
+        (reinterpret_cast<uintptr_t>(orow) & 15) == 0) {   // contiguous channel rows: float4 stores
+        for (int i4 = tid; 4 * i4 < KN; i4 += NT) {
+            const int i = 4 * i4, t = i >> logN, j = i & (N - 1);
+            float4 v = *reinterpret_cast<const float4*>(yo + (size_t)t * 2 * N + j);
+            if (tk.M > 1) v = f4add(v, *reinterpret_cast<const float4*>(emit + i));
+            *reinterpret_cast<float4*>(orow + t * rs.io.out_step + j) = v;
+        }
+        return;
+    }
     for (int i = tid; i < KN; i += NT) {
         const int t = i >> logN, j = i & (N - 1);
         float v = yo[(size_t)t * 2 * N + j];

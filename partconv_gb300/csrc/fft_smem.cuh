@@ -240,6 +240,26 @@ __device__ void fft_smem_pp(float2* s, float2* tmp, int N, int logN, const Twidd
     if (n2) stage_r2_pp<NT, MAXB>(a, b, N, Ns, lgNs, tw, inv);
 }
 
+// fft_smem_pp for a compile-time size N = 2^LOGN: the same stages in the same
+// order (identical results), unrolled with constant shifts and strides.
+template <int NT, int MAXB, int LOGN>
+__device__ __forceinline__ void fft_smem_pp_c(float2* s, float2* tmp, const float2* twtab, bool inv) {
+    constexpr int N = 1 << LOGN, n4 = LOGN >> 1, n2 = LOGN & 1;
+    constexpr bool odd = ((n4 + n2) & 1) != 0;
+    const Twiddles tw{twtab, LOGN};
+    float2* a = s;
+    float2* b = tmp;
+    if (odd) stage_r4<NT, MAXB>(s, N, 1, 0, tw, inv);   // odd stage count: one in-place stage first
+#pragma unroll
+    for (int st = odd ? 1 : 0; st < n4; ++st) {
+        stage_r4_pp<NT, MAXB>(a, b, N, 1 << (2 * st), 2 * st, tw, inv);
+        float2* t = a;
+        a = b;
+        b = t;
+    }
+    if (n2) stage_r2_pp<NT, MAXB>(a, b, N, 1 << (2 * n4), 2 * n4, tw, inv);
+}
+
 // Batched Stockham stages: K transforms of N points, transform t at
 // src + t N (dst + t N); the stage's K N / 4 (radix 4) or K N / 2 (radix 2)
 // butterflies are dealt round-robin over the CTA, so a CTA with more

@@ -271,8 +271,16 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     constexpr bool SW = !C::PREFETCH;
     // prefetch classes transform through the scratch buffer (fewer barriers)
     auto fft = [&](bool inv) {
-        if constexpr (C::PREFETCH) fft_smem_pp<NT, C::MAXB>(s, ftmp, N, logN, tw, inv);
-        else fft_smem<NT, C::MAXB, SW>(s, N, logN, tw, inv);
+        if constexpr (C::PREFETCH) {
+            switch (logN) {   // unrolled for the common base blocks; same results
+                case 7: fft_smem_pp_c<NT, C::MAXB, 7>(s, ftmp, twt, inv); break;
+                case 8: fft_smem_pp_c<NT, C::MAXB, 8>(s, ftmp, twt, inv); break;
+                case 9: fft_smem_pp_c<NT, C::MAXB, 9>(s, ftmp, twt, inv); break;
+                default: fft_smem_pp<NT, C::MAXB>(s, ftmp, N, logN, tw, inv);
+            }
+        } else {
+            fft_smem<NT, C::MAXB, SW>(s, N, logN, tw, inv);
+        }
     };
 
     const long long io_step = c - rs.io.step0;   // I/O is addressed by the global step

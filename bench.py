@@ -374,7 +374,8 @@ def run_ours(args):
     # live average duration per launch is the timed time over its launches.
     live_launch_s = (ms / 1e3) / (frames // (N0 * K))
     achieved = per_launch_b / live_launch_s / 1e9
-    traffic = ncu_traffic().get(dom["name"])
+    # captured per kernel kind and blocks per step (the K-block kernel is another instance)
+    traffic = ncu_traffic().get(dom["name"] if K == 1 else f"{dom['name']}@K{K}")
     kernels = {r["name"]: {"launches": r["launches"], "avg_us": r["total_ms"] * 1e3 / r["launches"],
                            "share": r["total_ms"] / sum(q["total_ms"] for q in prof),
                            "alg_bytes_per_launch": r["alg_bytes"] / r["launches"],

@@ -85,16 +85,17 @@ __global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs,
         float a = 0.f, b = 0.f;
         if (2 * n >= lo && 2 * n < hi && i >= 0 && i < jb.len) a = src[i];
         if (2 * n + 1 >= lo && 2 * n + 1 < hi && i + 1 >= 0 && i + 1 < jb.len) b = src[i + 1];
-        s[n] = make_float2(a, b);
+        s[sidx<true>(n)] = make_float2(a, b);
     }
-    load_twiddles<NT>(twt, logN, W, wlog);
+    load_twiddles_sw<NT>(twt, logN, W, wlog);
     __syncthreads();
     const Twiddles tw{twt, logN};
-    fft_smem<NT, MAXB>(s, N, logN, tw, false);
+    // transform buffer and twiddles in the conflict-free placement
+    fft_smem<NT, MAXB, true>(s, N, logN, tw, false);
     for (int k = threadIdx.x; k <= N / 2; k += NT) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
-        rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
+        rfft_split<true>(s[sidx<true>(k)], s[sidx<true>(nk)], k, logN, tw, xk, xnk);
         dst[k] = make_float2(xk.x * jb.scale, xk.y * jb.scale);
         if (N - k != k) dst[N - k] = make_float2(xnk.x * jb.scale, xnk.y * jb.scale);
     }
@@ -109,23 +110,24 @@ __global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs
     const IJob jb = jobs[blockIdx.x];
     const float2* src = reinterpret_cast<const float2*>(ptr.ws + jb.src_off);
     float* dst = ptr.out[jb.dst] + jb.dst_off;
-    load_twiddles<NT>(twt, logN, W, wlog);
+    load_twiddles_sw<NT>(twt, logN, W, wlog);
     __syncthreads();
     const Twiddles tw{twt, logN};
     for (int k = threadIdx.x; k <= N / 2; k += NT) {
         float2 zk, znk;
-        irfft_merge(src[k], src[N - k], k, logN, tw, zk, znk);
-        s[k] = zk;
-        if (k != 0 && k != N / 2) s[N - k] = znk;
+        irfft_merge<true>(src[k], src[N - k], k, logN, tw, zk, znk);
+        s[sidx<true>(k)] = zk;
+        if (k != 0 && k != N / 2) s[sidx<true>(N - k)] = znk;
     }
     __syncthreads();
-    fft_smem<NT, MAXB>(s, N, logN, tw, true);
-    const float* sf = reinterpret_cast<const float*>(s);
+    fft_smem<NT, MAXB, true>(s, N, logN, tw, true);
+    // real sample i is component i & 1 of complex element i >> 1
+    auto y = [&](int i) { return reinterpret_cast<const float*>(s + sidx<true>(i >> 1))[i & 1]; };
     const int n = jb.limit < N ? (int)jb.limit : N;
     for (int i = threadIdx.x; i < n; i += NT) {
-        if (jb.mode == 0) dst[i] = sf[i];
-        else if (jb.mode == 1) dst[i] += sf[i];
-        else dst[i] = sf[N - i] * jb.scale;
+        if (jb.mode == 0) dst[i] = y(i);
+        else if (jb.mode == 1) dst[i] += y(i);
+        else dst[i] = y(N - i) * jb.scale;
     }
 }
 

@@ -67,6 +67,14 @@ __device__ __forceinline__ void load_twiddles(float2* tab, int logN, const float
     for (int m = threadIdx.x; m < n; m += NT) tab[m] = __ldg(&W[m << sh]);
 }
 
+// load_twiddles for a table read in the conflict-free placement (Twiddles::get<true>)
+template <int NT>
+__device__ __forceinline__ void load_twiddles_sw(float2* tab, int logN, const float2* __restrict__ W, int wlog) {
+    const int n = 1 << (logN - 1);
+    const int sh = wlog - (logN + 1);
+    for (int m = threadIdx.x; m < n; m += NT) tab[twsw(m)] = __ldg(&W[m << sh]);
+}
+
 // Shared-memory placement of complex element i of a transform buffer.  With
 // SW the low four bits of i are XORed with 5 * ((i >> 4) & 3): a bijection
 // on every block of 64 elements under which the strided writes of the first

@@ -134,6 +134,7 @@ struct pc_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t side[kClasses] = {nullptr, nullptr, nullptr};   // graph-capture branches
     cudaStream_t aside[kClasses] = {nullptr, nullptr, nullptr};  // deferred fires (graph capture)
+    cudaStream_t cin = nullptr, cout = nullptr;   // pc_process copy pipeline
 
     int fs = 0, N0 = 0, n_in = 0, n_out = 0;
     int relaxed = 0;
@@ -240,6 +241,9 @@ void free_device(pc_handle* h) {
     }
     if (h->sside) cudaStreamDestroy(h->sside);
     h->sside = nullptr;
+    if (h->cin) cudaStreamDestroy(h->cin);
+    if (h->cout) cudaStreamDestroy(h->cout);
+    h->cin = h->cout = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     h->ready = false;
@@ -1041,7 +1045,10 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     return PC_OK;
 }
 
-IOView make_view(const pc_handle* h, const float* in, float* out, long long frames, int layout, long long step0) {
+// ch_stride: frames between channel rows of a planar buffer (0: frames)
+IOView make_view(const pc_handle* h, const float* in, float* out, long long frames, int layout, long long step0,
+                 long long ch_stride = 0) {
+    if (ch_stride <= 0) ch_stride = frames;
     IOView v;
     v.in = in;
     v.out = out;
@@ -1049,10 +1056,10 @@ IOView make_view(const pc_handle* h, const float* in, float* out, long long fram
     if (layout == PC_PLANAR) {
         v.in_step = h->N0;
         v.in_sample = 1;
-        v.in_ch = frames;
+        v.in_ch = ch_stride;
         v.out_step = h->N0;
         v.out_sample = 1;
-        v.out_ch = frames;
+        v.out_ch = ch_stride;
     } else {
         v.in_step = (long long)h->N0 * h->n_in;
         v.in_sample = h->n_in;
@@ -1307,6 +1314,60 @@ int pc_process(pc_handle* h, float* output, const float* input, long long frames
         h->big_out_cap = 0;
         CK(cudaMalloc(&h->d_big_out, sizeof(float) * nout), "output buffer");
         h->big_out_cap = nout;
+    }
+    // Long calls run as a pipeline of chunks: the input copy of chunk i + 1
+    // and the output copy of chunk i - 1 (own streams) overlap the steps of
+    // chunk i (the handle's stream); the steps of one call stay in order.
+    const long long chunk = (long long)std::max(h->G, 512) * h->N0;   // a multiple of KB N0
+    if (!h->relaxed && frames >= 2 * chunk) {
+        if (!h->cin) CK(cudaStreamCreateWithFlags(&h->cin, cudaStreamNonBlocking), "stream create");
+        if (!h->cout) CK(cudaStreamCreateWithFlags(&h->cout, cudaStreamNonBlocking), "stream create");
+        const bool planar = layout == PC_PLANAR;
+        const long long nch = (frames + chunk - 1) / chunk;
+        std::vector<cudaEvent_t> evs;
+        auto mkev = [&](cudaEvent_t* e) {
+            cudaError_t r = cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+            if (r == cudaSuccess) evs.push_back(*e);
+            return r;
+        };
+        int rc = PC_OK;
+        for (long long i = 0; i < nch && rc == PC_OK; ++i) {
+            const long long c0 = i * chunk, n = std::min(chunk, frames - c0);
+            cudaEvent_t ein, edone;
+            cudaError_t e = mkev(&ein);
+            if (e == cudaSuccess) e = mkev(&edone);
+            if (e == cudaSuccess)
+                e = planar ? cudaMemcpy2DAsync(h->d_big_in + c0, sizeof(float) * frames, input + c0, sizeof(float) * frames,
+                                               sizeof(float) * n, h->n_in, cudaMemcpyHostToDevice, h->cin)
+                           : cudaMemcpyAsync(h->d_big_in + c0 * h->n_in, input + c0 * h->n_in,
+                                             sizeof(float) * n * h->n_in, cudaMemcpyHostToDevice, h->cin);
+            if (e == cudaSuccess) e = cudaEventRecord(ein, h->cin);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, ein, 0);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(h, e, "input copy");
+                break;
+            }
+            const float* din = h->d_big_in + (planar ? c0 : c0 * h->n_in);
+            float* dout = h->d_big_out + (planar ? c0 : c0 * h->n_out);
+            IOView v = make_view(h, din, dout, n, layout, h->frame_num, frames);
+            rc = run_steps(h, v, n / h->N0, h->stream);
+            if (rc) break;
+            e = cudaEventRecord(edone, h->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->cout, edone, 0);
+            if (e == cudaSuccess)
+                e = planar ? cudaMemcpy2DAsync(output + c0, sizeof(float) * frames, h->d_big_out + c0, sizeof(float) * frames,
+                                               sizeof(float) * n, h->n_out, cudaMemcpyDeviceToHost, h->cout)
+                           : cudaMemcpyAsync(output + c0 * h->n_out, h->d_big_out + c0 * h->n_out,
+                                             sizeof(float) * n * h->n_out, cudaMemcpyDeviceToHost, h->cout);
+            if (e != cudaSuccess) rc = cuda_fail(h, e, "output copy");
+        }
+        cudaError_t e1 = cudaStreamSynchronize(h->cout);
+        cudaError_t e2 = cudaStreamSynchronize(h->stream);
+        for (auto ev : evs) cudaEventDestroy(ev);
+        if (rc) return rc;
+        if (e1 != cudaSuccess) return cuda_fail(h, e1, "process sync");
+        if (e2 != cudaSuccess) return cuda_fail(h, e2, "process sync");
+        return PC_OK;
     }
     CK(cudaMemcpyAsync(h->d_big_in, input, sizeof(float) * nin, cudaMemcpyHostToDevice, h->stream), "input copy");
     int r = process_device_impl(h, h->d_big_out, h->d_big_in, frames, layout, h->stream);

@@ -244,3 +244,35 @@ def test_rt_driver_matches_callbacks_and_reports(gpu):
     m.reset()
     y2, st2 = RealtimeDriver(m).run(x, realtime=False)
     assert np.array_equal(y2, y_cb) and st2["misses"] == 0
+
+
+@pytest.mark.parametrize("layout", [PC_INTERLEAVED, PC_PLANAR])
+def test_long_process_pipeline_equals_device_path(gpu, layout):
+    """A long pc_process call runs as chunks whose copies overlap the steps;
+    the result equals the unchunked device path bit for bit, for two inputs
+    mixed into three outputs."""
+    import torch
+
+    rng = np.random.default_rng(41)
+    N0 = 64
+    pcs = [dict(ir=_ir(rng, 9000), N=[64, 512, 4096], P=[14, 14, 0], in_ch=0, out_ch=0),
+           dict(ir=_ir(rng, 3000), N=[64, 256], P=[6, 0], in_ch=1, out_ch=0, scale=0.5),
+           dict(ir=_ir(rng, 5000), N=[64, 512], P=[10, 0], in_ch=1, out_ch=2)]
+    frames = N0 * 1500   # three chunks of 512 blocks (the last one shorter)
+    x = (0.1 * rng.standard_normal((frames, 2))).astype(np.float32)
+    xin = x if layout == PC_INTERLEAVED else np.ascontiguousarray(x.T)
+    a = PartConvMulti()
+    a.setup_layout(48000, N0, 2, 3, pcs)
+    ya = a.process(xin, layout)
+    b = PartConvMulti()
+    b.setup_layout(48000, N0, 2, 3, pcs)
+    xd = torch.from_numpy(xin).cuda()
+    yd = torch.empty(ya.shape, dtype=torch.float32, device="cuda")
+    b.process_device(yd, xd, frames, layout)
+    torch.cuda.synchronize()
+    assert np.array_equal(ya, yd.cpu().numpy())
+    yt = ya if layout == PC_INTERLEAVED else ya.T
+    ref = oracle.OracleMulti(N0, 2, 3, pcs).run(x)
+    for o in (0, 2):
+        assert wl.rel_l2(yt[:, o], ref[:, o]) <= TOL
+    assert np.all(yt[:, 1] == 0)

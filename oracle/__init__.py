@@ -1,7 +1,7 @@
 """CPU oracle for the partitioned-convolution path.
 
-TEST INFRASTRUCTURE ONLY: the checker the GPU path is compared against and the
-timed CPU baseline.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+TEST INFRASTRUCTURE ONLY: the reference the GPU path is compared against and
+the timed CPU baseline.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
 baseline legs of ``bench.py`` import this package.  The product library
 (``partconv_gb300``) never imports, links or calls it.
 

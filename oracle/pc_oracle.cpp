@@ -1,8 +1,8 @@
 // pc_oracle.cpp -- CPU restatement of partconv's multi-level partitioned
 // FFT convolution.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU path and
-// the timed CPU baseline.  Only tests, the smoke check and the benchmark's
+// TEST INFRASTRUCTURE ONLY.  This file is what the GPU path is compared
+// against, and the timed CPU baseline.  Only tests, the smoke check and the benchmark's
 // CPU-baseline leg load it; the product library never links or calls it.
 //
 // What is restated (file:line refer to ebattenberg/partconv):

@@ -85,6 +85,29 @@ def test_process_graph_path_equals_callbacks(gpu, N, P, L):
     assert np.array_equal(ya, yb)
 
 
+@pytest.mark.parametrize("N,P,L", [([64], [0], 40), ([64], [0], 100), ([64], [0], 180), ([64], [0], 250),
+                                   ([64, 128], [2, 0], 1500), ([64, 128], [3, 0], 1500), ([128, 256], [4, 0], 3000),
+                                   ([512, 1024], [3, 0], 5000)])
+def test_few_level0_parts(gpu, N, P, L):
+    """Level 0 with one to four parts, alone and under a larger level (the
+    one-block fire sums parts 0..2 itself, spread tasks the rest): long calls
+    and one call per block match the oracle and each other bit for bit.  A
+    long call transforms the two blocks before each block from its own
+    input, a one-block call reads them from the input ring."""
+    rng = np.random.default_rng(L + 7)
+    h = _ir(rng, L)
+    N0 = N[0]
+    frames = N0 * 60
+    x = (0.1 * rng.standard_normal((frames, 1))).astype(np.float32)
+    ref = oracle.OracleMulti(N0, 1, 1, [dict(ir=h, N=N, P=P)]).run(x)
+    m = PartConvMulti()
+    m.setup_layout(48000, N0, 1, 1, [dict(ir=h, N=N, P=P)])
+    y = np.concatenate([m.process(x[: 7 * N0]), m.process(x[7 * N0: 8 * N0]), m.process(x[8 * N0:])])
+    assert wl.rel_l2(y[:, 0], ref[:, 0]) <= TOL
+    m.reset()
+    assert np.array_equal(_run_callbacks(m, x, N0), y)
+
+
 def test_planar_equals_interleaved_and_mixing(gpu):
     rng = np.random.default_rng(21)
     N0 = 64

@@ -590,7 +590,9 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->sp_bytes.assign(NP, 0.0);
     for (int cls = 0; cls < kClasses; ++cls) h->alg_bytes[cls].assign(NP, 0.0);
     // order: larger fires first (longest CTAs start first), then level-0
-    // fires, then spread tasks
+    // fires, then spread tasks, also larger levels first (their slices read
+    // the most; measured 1 % faster on 32 streams of three levels than level
+    // 0 first)
     std::vector<int> order(nlv);
     for (int i = 0; i < nlv; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h->h_lv[a].N > h->h_lv[b].N; });
@@ -642,7 +644,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             h->alg_bytes[cls][g] += b;
         }
         const int sc = h->l0_class;
-        for (int li = 0; li < nlv; ++li) {
+        for (int li : order) {
             const DevLevel& l = h->h_lv[li];
             int lo, hi, p_lo;
             if (l.T == 1) {

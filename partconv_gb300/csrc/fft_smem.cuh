@@ -18,7 +18,9 @@
 // Twiddles come from a quarter-wave table in shared memory,
 // tw[m] = exp(-2 pi i m / 2N) for 0 <= m < N/2, filled once per CTA from a
 // global table computed in double on the host; other angles follow by
-// quarter-turn symmetry.
+// quarter-turn symmetry.  The radix-4 stages in the conflict-free placement
+// (the large transforms) read only w^k and form w^2k and w^3k by complex
+// products (about one float32 rounding more per factor).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -190,7 +192,8 @@ __device__ void fft_smem(float2* s, int N, int logN, const Twiddles& tw, bool in
 
 // Radix-4 and radix-2 Stockham stages from src to dst (a second buffer): one
 // barrier per stage instead of two, and the same arithmetic as the in-place
-// stages, so results are bit-identical.
+// stages in the plain placement (SW = false), so results are bit-identical
+// to those.
 template <int NT, int MAXB>
 __device__ __forceinline__ void stage_r4_pp(const float2* src, float2* dst, int N, int Ns, int lgNs,
                                             const Twiddles& tw, bool inv) {

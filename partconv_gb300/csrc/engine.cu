@@ -383,7 +383,12 @@ int build_graph(pc_handle* h) {
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     for (auto ev : evs) cudaEventDestroy(ev);
     if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->gexec, g, 0);
+    // with several base blocks per step the graph runs its nodes at their own
+    // priorities (chain high, deferred fires low): 61.3k against 60.3k
+    // audio-s/s on 32 streams; with one block per step that slowed the chain
+    // (58.0k against 59.6k), so it keeps the stream's priority
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&h->gexec, g, h->KB > 1 ? cudaGraphInstantiateFlagUseNodePriority : 0);
     if (g) cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(h, e, "graph capture");
     h->graph_kernels = kernels;

@@ -118,3 +118,27 @@ def test_cached_layout_lookup_and_fit(tmp_path):
         assert sum(n * p for n, p in zip(N, P)) >= L
     assert at.cached_layout(5000, 256, 32, cache=str(path)) is None
     assert at.cached_layout(100000, 128, 32, cache=str(path)) is None
+
+
+def test_shipped_cache_is_consistent():
+    """The cache shipped with the package: every key names a GPU, base block,
+    length class and batch class; its best layout is the fastest measured
+    candidate, and every stored layout is valid for its length class."""
+    import re
+
+    with open(autotune.DEFAULT_CACHE) as f:
+        db = json.load(f)
+    assert db
+    for key, rec in db.items():
+        m = re.fullmatch(r"(.+)\|N0=(\d+)\|len=(\d+)\|batch=(\d+)", key)
+        assert m, key
+        n0, lc = int(m.group(2)), int(m.group(3))
+        assert lc & (lc - 1) == 0
+        best = rec["best"]
+        cands = rec["candidates"]
+        assert cands and best in cands
+        assert best["us_per_step"] == min(c["us_per_step"] for c in cands)
+        for c in cands:
+            assert c["N"][0] == n0 and c["us_per_step"] > 0
+            st, _, _, msg = check_layout(c["N"], c["P"], lc)
+            assert st == 0, (key, c, msg)

@@ -185,6 +185,12 @@ def workload(streams: int, samples: int, layouts: str = "auto", measure: bool = 
     return c, x, frames
 
 
+def workload_name(streams: int, samples: int, frames1: int, N0: int) -> str:
+    """The cfg2 workload as both arms name it in ``config.workload``."""
+    return (f"cfg2: {streams} streams x {samples} samples + IR flush ({frames1} per stream), "
+            f"IR 2^14..2^19 taps, N0={N0}")
+
+
 def bytes_per_sample(layouts):
     from partconv_gb300 import workloads as wl
 
@@ -237,7 +243,7 @@ def run_reference(args):
         "value": v, "unit": "audio-s/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "cfg2: 32 streams x 2^19 samples, IR 2^14..2^19 taps, N0=256", "sample": sample},
+        "config": {"workload": workload_name(S, args.samples, frames, N0), "sample": sample},
         "cpu_baseline": {"value": v, "unit": "audio-s/s", "cores": threads, "kind": "port",
                          "sample": sample + "; restated CPU path (own FFT); reference FFTW build unavailable"},
         "e2e": {"value": v, "unit": "audio-s/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -449,9 +455,8 @@ def run_ours(args):
             "value": value, "unit": "audio-s/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded numpy PCG64, cfg seed 1002)",
-            "config": {"workload": f"cfg2: {S} streams x {args.samples} samples + IR flush ({frames1} per stream), "
-                                   f"IR 2^14..2^19 taps, N0={N0}, one handle, graph-replayed steps of "
-                                   f"{K} base block{'s' if K > 1 else ''}",
+            "config": {"workload": workload_name(S, args.samples, frames1, N0),
+                       "execution": f"one handle, graph-replayed steps of {K} base block{'s' if K > 1 else ''}",
                        "step_blocks": K,
                        "frames_processed_per_stream": frames,
                        "layouts": ("autotuned from measured GPU timings (partconv_gb300/autotune_cache.json)"
@@ -577,8 +582,8 @@ def run_adjoint(args):
     c = wl.cfg4()
     x = torch.from_numpy(c["x"]).cuda().requires_grad_(True)
     B, T = c["x"].shape
-    target = torch.from_numpy(np.stack([wl.conv_fp64(c["x"][b], c["h_target"], T) for b in range(B)])
-                              .astype(np.float32)).cuda()
+    t64 = np.stack([wl.conv_fp64(c["x"][b], c["h_target"], T) for b in range(B)])
+    target = torch.from_numpy(t64.astype(np.float32)).cuda()
     mod = PartitionedConv(c["h_init"], c["N"], c["P"], B, T).cuda()
     stream = torch.cuda.current_stream()
 
@@ -617,6 +622,15 @@ def run_adjoint(args):
 
     gx64, gh64 = dense(torch.float64)
     rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))  # noqa: E731
+    # FP64 central differences (step 1e-3) at 64 random IR taps and 64 random
+    # input samples; the last timed step's gradients (same IR, same inputs)
+    frng = np.random.default_rng(77)
+    ch = np.sort(frng.choice(len(c["h_init"]), 64, replace=False))
+    cx = [(int(b), int(i)) for b, i in zip(frng.integers(0, B, 64), frng.choice(T, 64, replace=False))]
+    fd_h, fd_x = wl.fd_grads_fp64(c["x"], c["h_init"], t64, ch, cx, 1e-3)
+    gh_np, gx_np = gh_ours.cpu().numpy(), gx_ours.cpu().numpy()
+    fd_err_h = wl.rel_l2(gh_np[ch], fd_h)
+    fd_err_x = wl.rel_l2(np.array([gx_np[b, i] for b, i in cx]), fd_x)
     for _ in range(2):
         dense(torch.float32)
     torch.cuda.synchronize()
@@ -636,7 +650,11 @@ def run_adjoint(args):
                       "gpu_launches": launches,
                       "parity": {"dL_dh_rel_l2_vs_dense_fp64": rel(gh_ours, gh64),
                                  "dL_dx_rel_l2_vs_dense_fp64": rel(gx_ours, gx64),
-                                 "how": "same inputs, IR and loss through torch.fft convolution autograd in float64"},
+                                 "dL_dh_rel_l2_vs_fd64": fd_err_h, "dL_dx_rel_l2_vs_fd64": fd_err_x,
+                                 "tol": 1e-6,
+                                 "how": "dense: same inputs, IR and loss through torch.fft convolution autograd in "
+                                        "float64; fd64: FP64 central differences, step 1e-3, 64 random IR taps "
+                                        "and 64 random input samples"},
                       "dense_torch_fft_fp32": {"ms_per_step": dense_ms, "value": audio / (dense_ms / 1e3),
                                                "unit": "audio-s/s"}}))
     return 0

@@ -389,19 +389,25 @@ void pcs_destroy(pcs_handle* h);
  * samples) are device pointers owned by the caller; enqueued on `stream`
  * (NULL = default stream), returns after enqueueing.
  *
- * All other working memory (filter spectra, spectrum ring, partial sums,
- * input ring, task table, twiddles) is one file-scope device array of
+ * All other working memory (twiddles, filter spectra, spectrum ring, partial
+ * sums, input ring, task table) is one file-scope device array of
  * PC_NOALLOC_SCRATCH_BYTES (32 MiB) that every GPU loading this library
- * holds until the process exits; the call allocates and frees nothing.  A
- * layout needing more (about 2 * 8 * h_len bytes plus 0.3 MiB; e.g. IRs of
- * up to ~1.9 M taps) fails with PC_ERR_LIMIT and a message from
- * pc_last_error(NULL).  block_size: a power of two in [16, 1024].
+ * holds until the process exits; the call allocates and frees nothing.  With
+ * P = ceil(h_len / block_size) parts and N = block_size, a call needs
+ *     262144 + 16 (N + 2)(P + 1) + 32 P + 192 (1 + ceil((N + 2) / 128)) + 8 N
+ * bytes, plus at most 2.5 KiB of 256-byte alignment: about 20 bytes per tap
+ * at N = 16 (IRs up to ~1.66 M taps) and 16 bytes per tap at N = 1024 (up to
+ * ~2.07 M taps).  A layout needing more fails with PC_ERR_LIMIT and a message
+ * from pc_last_error(NULL).  block_size: a power of two in [16, 1024].
  *
  * The first call on a device (that device current) resolves the array's
- * device address with cudaGetSymbolAddress; make that first call before any
- * stream capture.  Every call reuses the same array and clears the state it
- * needs, so calls that overlap on the GPU (different streams, or different
- * host threads on one device) race; serialise them.
+ * device address with cudaGetSymbolAddress and writes the twiddle table into
+ * it with a synchronous copy; make that first call before any stream
+ * capture.  Every call after it writes its tables with a kernel and reads no
+ * host memory, so it does not wait for earlier work on the stream.  Every
+ * call reuses the same array and clears the state it needs, so calls that
+ * overlap on the GPU (different streams, or different host threads on one
+ * device) race; serialise them.
  */
 int pc_convolve_noalloc(const float* d_x, long long n_frames, const float* d_h, int h_len, float* d_y,
                         int block_size, void* stream);

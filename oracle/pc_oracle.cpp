@@ -221,6 +221,10 @@ static int check_layout(int M, const int* N, int* P, int ir_len, bool relaxed,
     }
     if (delays) delays[M - 1] = (int)(position / N[0]);
     long rem = (long)ir_len - s;
+    // The reference refuses only rem < 0 (src/partconv.cpp:169-170).  With
+    // rem == 0 it sets P[M-1] = 0 and its runLevel then computes
+    // bcurr % num_parts (partconv.cpp:362), a division by zero; here the
+    // layout is refused instead, with the reference's message.
     if (rem <= 0) {
         snprintf(buf, sizeof buf, "last partitioning level (%d) not required", M);
         msg = buf;

@@ -13,6 +13,11 @@
 // file-scope __device__ memory that every GPU loading this library holds
 // until the process exits.  No call here allocates or frees device memory.
 //
+// The twiddle table is written once per device, by the first call on it,
+// at the front of the array.  Every later call writes its descriptor tables
+// with a one-CTA kernel from scalar launch arguments, so a call reads no
+// host memory and makes no host-to-device copy.
+//
 // The work is the step kernel of the multi-level engine run on a one-level
 // layout (block size N0, P = ceil(len(h) / N0) parts), so the result equals
 // pc_run over the same samples with a fresh handle.
@@ -56,6 +61,92 @@ size_t take(size_t& off, size_t bytes) {
     return o;
 }
 
+// Where each table sits in the scratch array, and what the table kernel
+// needs to write them (passed by value as the kernel's argument).
+struct TableArgs {
+    unsigned char* base;
+    const float* h;
+    int h_len, N, logN, P, cs, rin, nspread, spread_bins;
+    size_t o_W, o_pc, o_lv, o_mix, o_tasks, o_jobs, o_H, o_X, o_Yp, o_xr;
+};
+
+// Writes the one-level layout's descriptors: the PC, its level, the mixing
+// list of its single output, the fire task, the spread tasks (parts >= 2 in
+// slices of spread_bins bins) and one filter-spectrum job per part.
+__global__ void noalloc_tables_kernel(TableArgs a) {
+    float2* H = reinterpret_cast<float2*>(a.base + a.o_H);
+    float2* X = reinterpret_cast<float2*>(a.base + a.o_X);
+    float2* Yp = reinterpret_cast<float2*>(a.base + a.o_Yp);
+    float* xr = reinterpret_cast<float*>(a.base + a.o_xr);
+    Task* tasks = reinterpret_cast<Task*>(a.base + a.o_tasks);
+    SpectraJob* jobs = reinterpret_cast<SpectraJob*>(a.base + a.o_jobs);
+    if (threadIdx.x == 0) {
+        DevLevel lv{};
+        lv.N = a.N;
+        lv.logN = a.logN;
+        lv.P = a.P;
+        lv.T = 1;
+        lv.cs = a.cs;
+        lv.H = H;
+        lv.X = X;
+        lv.Yp = Yp;
+        *reinterpret_cast<DevLevel*>(a.base + a.o_lv) = lv;
+        DevPC pc{};
+        pc.M = 1;
+        pc.mix_mode = 1;
+        pc.scale = 1.0f;
+        pc.rin_mask = a.rin - 1;
+        pc.xring = xr;
+        *reinterpret_cast<DevPC*>(a.base + a.o_pc) = pc;
+        int* mix = reinterpret_cast<int*>(a.base + a.o_mix);   // out_off = {0, 1}, out_pcs = {0}
+        mix[0] = 0;
+        mix[1] = 1;
+        mix[2] = 0;
+        mix[3] = 0;
+        Task t{};
+        t.kind = 0;
+        t.N = a.N;
+        t.logN = a.logN;
+        t.P = a.P;
+        t.T = 1;
+        t.cs = a.cs;
+        t.M = 1;
+        t.mix_mode = 1;
+        t.rin_mask = a.rin - 1;
+        t.scale = 1.0f;
+        t.H = H;
+        t.X = X;
+        t.Yp = Yp;
+        t.xring = xr;
+        tasks[0] = t;
+    }
+    for (int s = threadIdx.x; s < a.nspread; s += blockDim.x) {
+        Task u{};
+        u.kind = 1;
+        u.N = a.N;
+        u.P = a.P;
+        u.T = 1;
+        u.cs = a.cs;
+        u.k0 = s * a.spread_bins;
+        u.k1 = min(a.cs, u.k0 + a.spread_bins);
+        u.p_lo = 2;
+        u.H = H;
+        u.X = X;
+        u.Yp = Yp;
+        tasks[1 + s] = u;
+    }
+    for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
+        const long start = (long)p * a.N;
+        SpectraJob j;
+        j.src = a.h + start;
+        j.len = (int)min((long)a.N, (long)a.h_len - start);
+        j.N = a.N;
+        j.logN = a.logN;
+        j.dst = H + (size_t)p * a.cs;
+        jobs[p] = j;
+    }
+}
+
 }  // namespace
 
 extern "C" int pc_convolve_noalloc(const float* d_x, long long n_frames, const float* d_h, int h_len, float* d_y,
@@ -67,28 +158,7 @@ extern "C" int pc_convolve_noalloc(const float* d_x, long long n_frames, const f
     if (h_len < 1) return fail(PC_ERR_ARG, "empty impulse response");
     cudaStream_t st = (cudaStream_t)stream;
 
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(PC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(PC_ERR_LIMIT, "device index beyond the supported range");
-    unsigned char* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch_addr[dev]) {
-            // first call on this device (it is the current device): resolve the
-            // device address of the scratch array
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_scratch);
-            if (e != cudaSuccess)
-                return fail(PC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            e = prepare_kernels();
-            if (e != cudaSuccess) return fail(PC_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(e));
-            g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-        }
-        base = g_scratch_addr[dev];
-    }
-
-    // ---- one-level layout and the scratch carve-up ---------------------------------
+    // ---- one-level layout and the scratch carve-up (twiddles first) -------------------
     const int N = block_size, logN = (int)std::lround(std::log2((double)N));
     const int P = (int)((h_len + N - 1) / N);
     const int cs = N + 2;
@@ -99,17 +169,18 @@ extern "C" int pc_convolve_noalloc(const float* d_x, long long n_frames, const f
     const int ntasks = 1 + nspread;
 
     size_t off = 0;
-    const size_t o_W = take(off, sizeof(float2) << kWlog);
-    const size_t o_pc = take(off, sizeof(DevPC));
-    const size_t o_lv = take(off, sizeof(DevLevel));
-    const size_t o_mix = take(off, 4 * sizeof(int));
-    const size_t o_tasks = take(off, sizeof(Task) * ntasks);
-    const size_t o_jobs = take(off, sizeof(SpectraJob) * (size_t)P);
-    const size_t o_H = take(off, sizeof(float2) * (size_t)P * cs);
+    TableArgs ta{};
+    ta.o_W = take(off, sizeof(float2) << kWlog);
+    ta.o_pc = take(off, sizeof(DevPC));
+    ta.o_lv = take(off, sizeof(DevLevel));
+    ta.o_mix = take(off, 4 * sizeof(int));
+    ta.o_tasks = take(off, sizeof(Task) * ntasks);
+    ta.o_jobs = take(off, sizeof(SpectraJob) * (size_t)P);
+    ta.o_H = take(off, sizeof(float2) * (size_t)P * cs);
     const size_t state0 = off;
-    const size_t o_X = take(off, sizeof(float2) * (size_t)P * cs);
-    const size_t o_Yp = take(off, sizeof(float2) * 2 * (size_t)cs);
-    const size_t o_xr = take(off, sizeof(float) * (size_t)Rin);
+    ta.o_X = take(off, sizeof(float2) * (size_t)P * cs);
+    ta.o_Yp = take(off, sizeof(float2) * 2 * (size_t)cs);
+    ta.o_xr = take(off, sizeof(float) * (size_t)Rin);
     const size_t state1 = off;
     if (off > kScratchBytes) {
         char buf[256];
@@ -119,103 +190,65 @@ extern "C" int pc_convolve_noalloc(const float* d_x, long long n_frames, const f
         return fail(PC_ERR_LIMIT, buf);
     }
 
-    // ---- host images of the tables ----------------------------------------------------
-    std::vector<float2> W((size_t)1 << kWlog);
-    for (size_t m = 0; m < W.size(); ++m) {
-        const double a = -2.0 * M_PI * (double)m / (double)W.size();
-        W[m] = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
-    DevLevel lv{};
-    lv.N = N;
-    lv.logN = logN;
-    lv.P = P;
-    lv.T = 1;
-    lv.s_blocks = 0;
-    lv.cs = cs;
-    lv.rmask = 0;
-    lv.pc = 0;
-    lv.H = reinterpret_cast<float2*>(base + o_H);
-    lv.X = reinterpret_cast<float2*>(base + o_X);
-    lv.Yp = reinterpret_cast<float2*>(base + o_Yp);
-    lv.yring = nullptr;
-    DevPC pc{};
-    pc.M = 1;
-    pc.lv0 = 0;
-    pc.mix_mode = 1;
-    pc.scale = 1.0f;
-    pc.rin_mask = Rin - 1;
-    pc.xring = reinterpret_cast<float*>(base + o_xr);
-    pc.pcout = nullptr;
-    int mix[4] = {0, 1, 0, 0};   // out_off = {0, 1}, out_pcs = {0}
-    std::vector<Task> tasks(ntasks);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(PC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return fail(PC_ERR_LIMIT, "device index beyond the supported range");
+    unsigned char* base = nullptr;
     {
-        Task& t = tasks[0];
-        t = Task{};
-        t.kind = 0;
-        t.N = N;
-        t.logN = logN;
-        t.P = P;
-        t.T = 1;
-        t.cs = cs;
-        t.M = 1;
-        t.mix_mode = 1;
-        t.rin_mask = Rin - 1;
-        t.scale = 1.0f;
-        t.H = lv.H;
-        t.X = lv.X;
-        t.Yp = lv.Yp;
-        t.xring = pc.xring;
-        for (int s = 0; s < nspread; ++s) {
-            Task& u = tasks[1 + s];
-            u = Task{};
-            u.kind = 1;
-            u.N = N;
-            u.P = P;
-            u.T = 1;
-            u.cs = cs;
-            u.k0 = s * spread_task_bins();
-            u.k1 = std::min(cs, u.k0 + spread_task_bins());
-            u.p_lo = 2;
-            u.H = lv.H;
-            u.X = lv.X;
-            u.Yp = lv.Yp;
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!g_scratch_addr[dev]) {
+            // first call on this device (it is the current device): resolve the
+            // device address of the scratch array and write the twiddle table
+            // exp(-2 pi i m / 2^15), computed in double like the engine's, at
+            // its front once (a synchronous copy)
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_scratch);
+            if (e != cudaSuccess)
+                return fail(PC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            e = prepare_kernels();
+            if (e != cudaSuccess) return fail(PC_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(e));
+            std::vector<float2> W((size_t)1 << kWlog);
+            for (size_t m = 0; m < W.size(); ++m) {
+                const double a = -2.0 * M_PI * (double)m / (double)W.size();
+                W[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+            }
+            e = cudaMemcpy(p, W.data(), sizeof(float2) * W.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return fail(PC_ERR_CUDA, std::string("twiddle upload: ") + cudaGetErrorString(e));
+            g_scratch_addr[dev] = static_cast<unsigned char*>(p);
         }
-    }
-    std::vector<SpectraJob> jobs(P);
-    for (int p = 0; p < P; ++p) {
-        const long start = (long)p * N;
-        jobs[p].src = d_h + start;
-        jobs[p].len = (int)std::min<long>(N, (long)h_len - start);
-        jobs[p].N = N;
-        jobs[p].logN = logN;
-        jobs[p].dst = lv.H + (size_t)p * cs;
+        base = g_scratch_addr[dev];
     }
 
-    // ---- uploads (pageable host sources are staged by the driver before the
-    //      call returns), clear the state, filter spectra, steps ------------------
-    auto cp = [&](size_t o, const void* src, size_t bytes) {
-        return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, st);
-    };
-    if ((e = cp(o_W, W.data(), sizeof(float2) * W.size())) != cudaSuccess ||
-        (e = cp(o_pc, &pc, sizeof pc)) != cudaSuccess || (e = cp(o_lv, &lv, sizeof lv)) != cudaSuccess ||
-        (e = cp(o_mix, mix, sizeof mix)) != cudaSuccess ||
-        (e = cp(o_tasks, tasks.data(), sizeof(Task) * tasks.size())) != cudaSuccess ||
-        (e = cp(o_jobs, jobs.data(), sizeof(SpectraJob) * jobs.size())) != cudaSuccess ||
+    // ---- descriptor tables (a kernel: no host memory is read), cleared state,
+    //      filter spectra, steps ------------------------------------------------------------
+    ta.base = base;
+    ta.h = d_h;
+    ta.h_len = h_len;
+    ta.N = N;
+    ta.logN = logN;
+    ta.P = P;
+    ta.cs = cs;
+    ta.rin = Rin;
+    ta.nspread = nspread;
+    ta.spread_bins = spread_task_bins();
+    noalloc_tables_kernel<<<1, 256, 0, st>>>(ta);
+    if ((e = cudaGetLastError()) != cudaSuccess ||
         (e = cudaMemsetAsync(base + state0, 0, state1 - state0, st)) != cudaSuccess)
-        return fail(PC_ERR_CUDA, std::string("scratch upload: ") + cudaGetErrorString(e));
-    e = launch_spectra(cls, P, N, reinterpret_cast<const SpectraJob*>(base + o_jobs),
-                       reinterpret_cast<const float2*>(base + o_W), kWlog, st);
+        return fail(PC_ERR_CUDA, std::string("scratch tables: ") + cudaGetErrorString(e));
+    e = launch_spectra(cls, P, N, reinterpret_cast<const SpectraJob*>(base + ta.o_jobs),
+                       reinterpret_cast<const float2*>(base + ta.o_W), kWlog, st);
     if (e != cudaSuccess) return fail(PC_ERR_CUDA, std::string("filter spectra: ") + cudaGetErrorString(e));
 
     Bank bank{};
-    bank.pcs = reinterpret_cast<const DevPC*>(base + o_pc);
-    bank.lv = reinterpret_cast<const DevLevel*>(base + o_lv);
-    bank.W = reinterpret_cast<const float2*>(base + o_W);
+    bank.pcs = reinterpret_cast<const DevPC*>(base + ta.o_pc);
+    bank.lv = reinterpret_cast<const DevLevel*>(base + ta.o_lv);
+    bank.W = reinterpret_cast<const float2*>(base + ta.o_W);
     bank.wlog = kWlog;
     bank.N0 = N;
     bank.n_out = 1;
-    bank.out_off = reinterpret_cast<const int*>(base + o_mix);
-    bank.out_pcs = reinterpret_cast<const int*>(base + o_mix) + 2;
+    bank.out_off = reinterpret_cast<const int*>(base + ta.o_mix);
+    bank.out_pcs = reinterpret_cast<const int*>(base + ta.o_mix) + 2;
     bank.mix_cnt = nullptr;
     bank.zero_list = nullptr;
     RunState rs{};
@@ -229,7 +262,7 @@ extern "C" int pc_convolve_noalloc(const float* d_x, long long n_frames, const f
     rs.io.out_sample = 1;
     rs.io.out_ch = 0;
     const long long nsteps = n_frames / N;
-    const Task* d_tasks = reinterpret_cast<const Task*>(base + o_tasks);
+    const Task* d_tasks = reinterpret_cast<const Task*>(base + ta.o_tasks);
     for (long long c = 0; c < nsteps; ++c) {
         rs.step_base = c;
         // the first step follows the spectra kernel, so it must not overlap it

@@ -5,7 +5,8 @@ wraps src/partconv.h): ``PartConvFilter``, ``PartConvMax``, ``DelayBuffer``,
 ``DoubleBuffer``, ``intArray`` and ``doubleArray``, plus ``PartConvMulti``
 (not wrapped by the reference's SWIG file; added here for the multi-instance
 drop-in).  Scripts written against the reference module, e.g. src/tune.py,
-run after ``from partconv_gb300 import partconv``.
+run after ``import partconv`` (the top-level module of this repository) or
+``from partconv_gb300 import partconv``.
 
 Error behaviour follows the reference where it returns codes
 (``PartConvFilter.setup`` returns 1 for a rejected layout); where the

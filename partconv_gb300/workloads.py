@@ -147,3 +147,37 @@ def algorithmic_bytes_per_sample(N, P) -> float:
     sum_L B_L / N_L with B_L = 8 (N_L + 1)(2 P_L + 1) + 12 N_L (read H and
     the X ring, write the new X slot, read 2N inputs, write N outputs)."""
     return sum((8.0 * (n + 1) * (2 * p + 1) + 12.0 * n) / n for n, p in zip(N, P))
+
+
+def fd_grads_fp64(x: np.ndarray, h: np.ndarray, target: np.ndarray, coords_h, coords_x, step: float = 1e-3):
+    """FP64 central differences of L = mean((conv(x_b, h)[:T] - target_b)^2)
+    over a batch x [B, T], at the IR taps ``coords_h`` and the input samples
+    ``coords_x`` (pairs (b, i)), step ``step``.
+
+    y is linear in h and in x, so L(h +- d e_j) only moves the residual by
+    +- d x_b shifted by j, and L(x +- d e_(b,i)) moves row b by +- d h
+    shifted by i; each difference (L+ - L-) / 2d is evaluated from those two
+    loss values in float64.  Returns (dL/dh at coords_h, dL/dx at coords_x)."""
+    x64 = np.asarray(x, np.float64)
+    h64 = np.asarray(h, np.float64)
+    B, T = x64.shape
+    r = np.stack([conv_fp64(x64[b], h64, T) for b in range(B)]) - np.asarray(target, np.float64)
+    M = r.size
+    gh = np.empty(len(coords_h))
+    for n, j in enumerate(coords_h):
+        xs = np.zeros_like(x64)
+        xs[:, j:] = x64[:, : T - j]
+        lp = np.sum((r + step * xs) ** 2) / M
+        lm = np.sum((r - step * xs) ** 2) / M
+        gh[n] = (lp - lm) / (2 * step)
+    gx = np.empty(len(coords_x))
+    L = len(h64)
+    for n, (b, i) in enumerate(coords_x):
+        hs = np.zeros(T)
+        m = min(L, T - i)
+        hs[i:i + m] = h64[:m]
+        # rows other than b are unchanged and cancel exactly in L+ - L-
+        lp = np.sum((r[b] + step * hs) ** 2) / M
+        lm = np.sum((r[b] - step * hs) ** 2) / M
+        gx[n] = (lp - lm) / (2 * step)
+    return gh, gx

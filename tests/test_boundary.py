@@ -236,3 +236,18 @@ def test_delay_and_double_buffer_semantics(gpu):
     assert float(dbuf.getReadBuffer().sum()) == 16.0
     dbuf.reset()
     assert float(dbuf.getReadBuffer().sum()) == 0.0
+
+
+def test_top_level_partconv_module_name():
+    """``import partconv`` -- the reference binding's module name
+    (src/partconv.i:3), imported by src/tune.py:2 -- gives the same classes as
+    partconv_gb300.partconv."""
+    import importlib
+
+    top = importlib.import_module("partconv")
+    for name in ("PartConvFilter", "PartConvMax", "DelayBuffer", "DoubleBuffer", "intArray", "doubleArray",
+                 "PartConvMulti"):
+        assert getattr(top, name) is getattr(partconv, name)
+    a = top.intArray(4)
+    a[2] = 7
+    assert a[2] == 7 and top.doubleArray(2)[1] == 0.0

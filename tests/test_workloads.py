@@ -73,3 +73,23 @@ def test_serving_layouts_are_valid():
             N, P = serving_layout(L, n0)
             assert N[0] == n0 and len(N) <= 5 and N[-1] <= 16384
             assert check_layout(N, P, L)[0] == 0, (L, n0, N, P)
+
+
+def test_fd_grads_fp64_match_analytic_gradients():
+    """The FP64 central differences that check the adjoint equal the exact
+    gradients of the quadratic loss: dL/dh_j = 2/M sum r_b[n] x_b[n-j] and
+    dL/dx_(b,i) = 2/M sum_n r_b[n] h[n-i]."""
+    rng = np.random.default_rng(3)
+    B, T, L = 2, 300, 50
+    x = (0.1 * rng.standard_normal((B, T))).astype(np.float32)
+    h = (0.01 * rng.standard_normal(L)).astype(np.float32)
+    t = rng.standard_normal((B, T)) * 0.1
+    r = np.stack([np.convolve(x[b].astype(np.float64), h.astype(np.float64))[:T] for b in range(B)]) - t
+    M = r.size
+    ch = [0, 7, 49]
+    cx = [(0, 0), (1, 120), (1, 299)]
+    gh, gx = wl.fd_grads_fp64(x, h, t, ch, cx, 1e-3)
+    ref_h = [2 / M * sum(np.dot(r[b, j:], x[b, : T - j].astype(np.float64)) for b in range(B)) for j in ch]
+    ref_x = [2 / M * np.dot(r[b, i:i + L][: T - i], h[: T - i].astype(np.float64)) for b, i in cx]
+    assert np.allclose(gh, ref_h, rtol=1e-9, atol=0)
+    assert np.allclose(gx, ref_x, rtol=1e-9, atol=0)

@@ -26,13 +26,19 @@ def _noalloc(x_d, h_d, y_d, frames, h_len, n0, stream):
                                          C.c_void_p(y_d.data_ptr()), n0, C.c_void_p(stream))
 
 
-def test_noalloc_matches_engine_on_two_calls(gpu):
+# (block size, IR taps): two multi-part layouts with spread tasks (P >= 3),
+# then the smallest and largest block sizes with P = 2 and a one-part IR, so
+# the path without spread tasks runs too
+CASES = [(128, 7000), (256, 20000), (16, 20), (1024, 1500), (64, 50)]
+
+
+def test_noalloc_matches_engine_on_consecutive_calls(gpu):
     import torch
 
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev).cuda_stream
     rng = np.random.default_rng(1234)
-    for call, (n0, h_len) in enumerate([(128, 7000), (256, 20000)]):
+    for call, (n0, h_len) in enumerate(CASES):
         h = wl.decaying_ir(rng, h_len, 0.3)
         frames = n0 * (h_len // n0 + 48)
         x = (0.1 * rng.standard_normal(frames)).astype(np.float32)
@@ -51,8 +57,33 @@ def test_noalloc_matches_engine_on_two_calls(gpu):
         a = y.cpu().numpy()
         b = y_ref.cpu().numpy()
         assert np.all(np.isfinite(a)), f"call {call}: unwritten output"
-        assert wl.rel_l2(a, b) <= TOL, f"call {call}: rel L2 {wl.rel_l2(a, b):.3e}"
+        assert wl.rel_l2(a, b) <= TOL, f"call {call} ({n0}, {h_len}): rel L2 {wl.rel_l2(a, b):.3e}"
         assert wl.rel_l2(a, wl.conv_fp64(x, h, frames)) <= TOL
+
+
+def test_noalloc_call_leaves_device_memory_unchanged(gpu):
+    """After a first call on the device, a call takes no device memory: the
+    free memory the driver reports is the same before and after it, and the
+    repeated call gives the same bits."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rng = np.random.default_rng(99)
+    n0, h_len = 256, 30000
+    h_d = torch.from_numpy(wl.decaying_ir(rng, h_len, 0.5)).to(dev)
+    frames = n0 * 200
+    x_d = torch.from_numpy((0.1 * rng.standard_normal(frames)).astype(np.float32)).to(dev)
+    y1 = torch.empty_like(x_d)
+    y2 = torch.empty_like(x_d)
+    assert _noalloc(x_d, h_d, y1, frames, h_len, n0, stream) == nat.PC_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    assert _noalloc(x_d, h_d, y2, frames, h_len, n0, stream) == nat.PC_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0
+    assert torch.equal(y1, y2)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):

@@ -19,8 +19,8 @@ _i32p = C.POINTER(C.c_int)
 
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the Makefile beside this file."""
-    src = os.path.join(_HERE, "pc_oracle.cpp")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("pc_oracle.cpp", "orc_fft.h")]
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(map(os.path.getmtime, srcs)):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 

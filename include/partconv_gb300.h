@@ -41,8 +41,11 @@ extern "C" {
 #define PC_INTERLEAVED 0
 #define PC_PLANAR 1
 
-/* Largest block size a level may use (the FFT length is twice this). */
-#define PC_MAX_BLOCK 16384
+/* Largest block size a level may use (the FFT length is twice this).  The
+ * pc_* engine transforms blocks above 16384 with a cluster of CTAs; the
+ * MIMO (pcm_*), differentiable (pcd_*), serving (pcs_*) and PartConvFilter
+ * (pcf_*) paths take blocks up to 16384 and return PC_ERR_LIMIT above. */
+#define PC_MAX_BLOCK 65536
 /* Most levels one convolver may have. */
 #define PC_MAX_LEVELS 16
 
@@ -182,8 +185,9 @@ long long pc_kernel_launches(const pc_handle* h);
 
 /* Per-kernel timing record filled by pc_profile_kernels. */
 typedef struct pc_kernel_stats {
-    char name[32];         /* "step_small", "step_mid", "step_large": the step kernel of
-                              block-size class N <= 1024, <= 4096, <= 16384 */
+    char name[32];         /* "step_small", "step_mid", "step_large", "step_huge": the step
+                              kernel of block-size class N <= 1024, <= 4096, <= 16384,
+                              <= 65536 (a cluster of 8 CTAs per fire); "spread_side" */
     long long launches;    /* launches that had work in their phase */
     double total_ms;       /* CUDA-event time summed over those launches */
     double alg_bytes;      /* algorithmic bytes those launches had to move */

@@ -22,7 +22,7 @@ PC_ERR_STATE = 7
 PC_ERR_LIMIT = 8
 PC_INTERLEAVED = 0
 PC_PLANAR = 1
-PC_MAX_BLOCK = 16384
+PC_MAX_BLOCK = 65536
 PC_MAX_LEVELS = 16
 PC_NOALLOC_SCRATCH_BYTES = 32 << 20
 

@@ -506,6 +506,10 @@ pcd_plan* pcd_create(int M, const int* N, int* P, int ir_len, int batch, long lo
         put(m2);
         return nullptr;
     }
+    if (Nv[M - 1] > kMaxBlockOneCta) {
+        put("differentiable levels are limited to blocks of 16384 (larger blocks: pc_* engine)");
+        return nullptr;
+    }
     if (Nv[0] < 16) {
         put("block size of level 0 must be >= 16");
         return nullptr;

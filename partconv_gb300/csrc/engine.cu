@@ -34,10 +34,10 @@ using namespace pcg;
 
 namespace {
 
-constexpr int kWlog = 15;          // twiddle table 2^15 entries: real FFTs up to 2 * 16384
+constexpr int kWlog = 17;          // twiddle table 2^17 entries: real FFTs up to 2 * 65536
 constexpr int kMinGraphSteps = 64; // base steps per captured graph (a multiple of the hyperperiod)
 constexpr int kMinN0 = 16;
-constexpr int kClasses = 3;
+constexpr int kClasses = kNumClasses;
 
 bool is_pow2(long x) { return x > 0 && (x & (x - 1)) == 0; }
 int ilog2(long x) {
@@ -136,8 +136,8 @@ struct pc_handle {
     bool ready = false;
     int device = -1;
     cudaStream_t stream = nullptr;
-    cudaStream_t side[kClasses] = {nullptr, nullptr, nullptr};   // graph-capture branches
-    cudaStream_t aside[kClasses] = {nullptr, nullptr, nullptr};  // deferred fires (graph capture)
+    cudaStream_t side[kClasses] = {};    // graph-capture branches
+    cudaStream_t aside[kClasses] = {};   // deferred fires (graph capture)
     cudaStream_t cin = nullptr, cout = nullptr;   // pc_process copy pipeline
 
     int fs = 0, N0 = 0, n_in = 0, n_out = 0;
@@ -180,7 +180,7 @@ struct pc_handle {
     cudaStream_t sside = nullptr;
     std::vector<int> sp_off, sp_cnt;
     std::vector<double> sp_bytes;
-    int class_maxN[kClasses] = {0, 0, 0};
+    int class_maxN[kClasses] = {};
     RunState* d_rs = nullptr;
 
     // run() staging and Relaxed carry (planar [n_out][N0])
@@ -1457,7 +1457,7 @@ int pc_profile_kernels(pc_handle* h, long long nsteps, pc_kernel_stats* out, int
     if (nsteps < 1 || !out || max_kinds < 1) return fail(h, PC_ERR_ARG, "bad profile arguments");
     CK(cudaSetDevice(h->device), "cudaSetDevice");
     constexpr int kKinds = kClasses + 1;   // + the side spread launches
-    static const char* names[kKinds] = {"step_small", "step_mid", "step_large", "spread_side"};
+    static const char* names[kKinds] = {"step_small", "step_mid", "step_large", "step_huge", "spread_side"};
     struct Rec {
         int cls;
         int phase;

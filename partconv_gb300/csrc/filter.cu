@@ -256,6 +256,8 @@ int pcf_setup(pcf_handle* h, int M, const int* N, int* P, const float* ir, int i
     char msg[256];
     int r = pc_check_layout(M, Nv.data(), Pv.data(), (int)hv.size(), relaxed_check, delays.data(), msg, sizeof msg);
     if (r) return ffail(h, r, msg);
+    if (Nv[M - 1] > kMaxBlockOneCta)
+        return ffail(h, PC_ERR_LIMIT, "PartConvFilter levels are limited to blocks of 16384 (larger blocks: pc_* engine)");
     for (int i = 0; i < M; ++i) P[i] = Pv[i];
     if (Nv[0] < 16) return ffail(h, PC_ERR_LIMIT, "block size of level 0 must be >= 16");
     FCK(cudaGetDevice(&h->device), "cudaGetDevice");

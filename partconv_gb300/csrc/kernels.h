@@ -18,8 +18,13 @@ struct SpectraJob {
     float2* dst;
 };
 
-// kernel class by block size: 0 (N <= 1024), 1 (N <= 4096), 2 (N <= 16384)
+// kernel class by block size: 0 (N <= 1024), 1 (N <= 4096), 2 (N <= 16384),
+// 3 (N <= 65536: a cluster of kClusterCtas CTAs per fire, cluster_fire.cu)
 int fire_class_of(int N);
+constexpr int kNumClasses = 4;
+constexpr int kMaxBlockOneCta = 16384;   // largest block one CTA transforms (classes 0-2)
+constexpr int kClusterCtas = 8;          // CTAs per class-3 fire
+constexpr int kClusterMaxN = 65536;      // largest block of class 3
 // threads per CTA of a class
 int class_threads(int cls);
 // bins one spread task covers
@@ -53,6 +58,14 @@ cudaError_t launch_pool_class(int cls, int grid, int maxN, const Bank& bank, con
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,
                            cudaStream_t st);
 cudaError_t launch_set_state(RunState* dst, const RunState& v, cudaStream_t st);
+
+// class 3 (cluster_fire.cu): fires and filter spectra of levels with
+// 16384 < N <= 65536, one cluster of kClusterCtas CTAs per task or job
+size_t cluster_smem_bytes();
+cudaError_t prepare_cluster_kernels();
+cudaError_t launch_cluster_fire(int ntasks, const Bank& bank, const Task* tasks, const RunState& rs,
+                                const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio);
+cudaError_t launch_cluster_spectra(int njobs, const SpectraJob* jobs, const float2* W, int wlog, cudaStream_t st);
 
 }  // namespace pcg
 

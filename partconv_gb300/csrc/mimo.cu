@@ -495,6 +495,8 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
     char msg[256];
     int r = pc_check_layout(M, Nv.data(), Pv.data(), ir_len, 1, nullptr, msg, sizeof msg);
     if (r) return mfail(h, r, msg);
+    if (Nv[M - 1] > kMaxBlockOneCta)
+        return mfail(h, PC_ERR_LIMIT, "MIMO levels are limited to blocks of 16384 (larger blocks: pc_* engine)");
     for (int i = 0; i < M; ++i) P[i] = Pv[i];
     MCK(cudaGetDevice(&h->device), "cudaGetDevice");
     MCK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");

@@ -287,6 +287,8 @@ int pcs_admit_async(pcs_handle* h, const float* ir, int ir_len, int M, const int
     char msg[256];
     int r = pc_check_layout(M, Nv.data(), Pv.data(), ir_len, 1, nullptr, msg, sizeof msg);
     if (r) return sfail(h, r, msg);
+    if (Nv[M - 1] > kMaxBlockOneCta)
+        return sfail(h, PC_ERR_LIMIT, "serving levels are limited to blocks of 16384 (larger blocks: pc_* engine)");
     for (int i = 0; i < M; ++i) P[i] = Pv[i];
     int id = -1;
     for (int i = 0; i < h->max_pcs; ++i)

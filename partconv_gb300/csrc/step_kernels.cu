@@ -1171,15 +1171,17 @@ __global__ void set_state_kernel(RunState* dst, RunState v) { *dst = v; }
 // ---------------------------------------------------------------------------
 // Host-side launchers.
 // ---------------------------------------------------------------------------
-int fire_class_of(int N) { return N <= Cls0::MAXN ? 0 : (N <= Cls1::MAXN ? 1 : 2); }
+int fire_class_of(int N) { return N <= Cls0::MAXN ? 0 : (N <= Cls1::MAXN ? 1 : (N <= Cls2::MAXN ? 2 : 3)); }
+static_assert(Cls2::MAXN == kMaxBlockOneCta, "class 2 is the largest one-CTA class");
 
 static const int kNT[3] = {Cls0::NT, Cls1::NT, Cls2::NT};
 static const bool kPrefetch[3] = {Cls0::PREFETCH, Cls1::PREFETCH, Cls2::PREFETCH};
-int class_threads(int cls) { return kNT[cls]; }
+int class_threads(int cls) { return cls == 3 ? 512 : kNT[cls]; }
 int spread_task_bins() { return 2 * kSpreadLanes; }
 int spread_task_parts() { return kSpreadParts; }
 
 size_t class_smem_bytes(int cls, int maxN) {
+    if (cls == 3) return cluster_smem_bytes();
     size_t b = fire_smem_bytes(maxN, kPrefetch[cls]);
     const size_t red = sizeof(float4) * (size_t)kNT[cls];   // spread part-group partials
     return b > red ? b : red;
@@ -1205,7 +1207,8 @@ int max_step_blocks(int N0) {
 }
 
 cudaError_t prepare_kernels() {
-    cudaError_t e;
+    cudaError_t e = prepare_cluster_kernels();
+    if (e != cudaSuccess) return e;
     size_t s0 = class_smem_bytes(0, Cls0::MAXN);
     for (int N = 16; N <= Cls0::MAXN; N *= 2)
         for (int k = 2; k <= max_step_blocks(N); k *= 2) s0 = std::max(s0, multi_smem_bytes(N, k, multi_fire_parts(N, k)));
@@ -1238,6 +1241,7 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
                               const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio,
                               bool whole_sm) {
     if (grid <= 0) return cudaSuccess;
+    if (cls == 3) return launch_cluster_fire(grid, bank, tasks, rs, rs_dev, step_in_batch, st, pdl, prio);
     static int least = 0, greatest = 0;
     static const bool have_range = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess;
     // programmatic dependent launch: this step's CTAs may be scheduled while
@@ -1278,6 +1282,7 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
 cudaError_t launch_spectra(int cls, int njobs, int maxN, const SpectraJob* jobs, const float2* W, int wlog,
                            cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
+    if (cls == 3) return launch_cluster_spectra(njobs, jobs, W, wlog, st);
     const size_t smem = (size_t)12 * maxN;
     switch (cls) {
         case 0: spectra_kernel<128, 2><<<njobs, 128, smem, st>>>(jobs, W, wlog); break;

@@ -76,7 +76,11 @@ def test_layout_check_agrees_with_oracle(relaxed):
 
 
 def test_layout_limits():
-    st, _, _, msg = check_layout([256, 2048, 32768], [8, 7, 2], 200000)
+    # blocks up to 65536 (a 131072-point real transform) are accepted, the
+    # next power of two is not
+    st, P, _, msg = check_layout([256, 2048, 16384, 65536], [8, 7, 7, 1], 300000)
+    assert st == 0 and P[-1] == 3, msg
+    st, _, _, msg = check_layout([256, 2048, 16384, 131072], [8, 7, 7, 1], 300000)
     assert st == nat.PC_ERR_LIMIT and "limit" in msg
     st, _, _, msg = check_layout([16] * 17, [1] * 17, 1000)
     assert st == nat.PC_ERR_LIMIT

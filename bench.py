@@ -276,7 +276,13 @@ def run_ours(args):
     frames = frames1 if K == 1 else frames_pad
     x_host = np.ascontiguousarray(x_pad[:, :frames])
     pcs = [dict(ir=h, N=N, P=P, in_ch=s, out_ch=s) for s, (h, (N, P)) in enumerate(zip(c["irs"], c["layouts"]))]
-    m = PartConvMulti(step_blocks=K)
+    # kernel tile shape for this handle: the autotuner's measured choice (cached)
+    tiles = None
+    if args.layouts == "auto":
+        from partconv_gb300 import autotune
+
+        tiles = autotune.choose_tiles(pcs, N0, "cfg2", measure=True)
+    m = PartConvMulti(step_blocks=K, tiles=tiles)
     m.setup_layout(FS, N0, S, S, pcs)
     info = m.info()
     K = info.step_blocks
@@ -333,7 +339,7 @@ def run_ours(args):
     #      or one launch per block when the headline uses K > 1) ---------------
     alt = None
     if not args.no_alt:
-        m1 = PartConvMulti(step_blocks=ALT)
+        m1 = PartConvMulti(step_blocks=ALT, tiles=tiles)
         m1.setup_layout(FS, N0, S, S, pcs)
         alt_k = m1.info().step_blocks
         n_alt = frames_pad if alt_k > 1 else frames1
@@ -458,9 +464,13 @@ def run_ours(args):
             "config": {"workload": workload_name(S, args.samples, frames1, N0),
                        "execution": f"one handle, graph-replayed steps of {K} base block{'s' if K > 1 else ''}",
                        "step_blocks": K,
+                       "tiles": {"spread_bins": info.spread_bins, "spread_parts": info.spread_parts,
+                                 "how": "bins and parts per spread task, measured by the autotuner on this handle"
+                                        if tiles else "default"},
                        "frames_processed_per_stream": frames,
                        "layouts": ("autotuned from measured GPU timings (partconv_gb300/autotune_cache.json)"
                                    if args.layouts == "auto" else "minimum-slack level chain (ratio 8, max 16384)"),
+                       "max_block": max(max(N) for N, _ in c["layouts"]),
                        "layout_set": sorted({f"{N}x{P}" for N, P in c["layouts"]})[:8],
                        "streams": S, "frames_per_stream": frames, "N0": N0,
                        "hyperperiod_steps": info.hyperperiod,

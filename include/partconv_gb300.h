@@ -64,6 +64,8 @@ typedef struct pc_info {
     long long frame_num;     /* run() calls so far (PartConvMulti::frameNum) */
     long long device_bytes;  /* device memory held by the handle */
     int step_blocks;         /* base blocks computed per step (pc_set_step_blocks) */
+    int spread_bins;         /* bins per spread task in use (pc_set_tiles) */
+    int spread_parts;        /* parts per spread task in use (pc_set_tiles) */
 } pc_info;
 
 /*
@@ -132,6 +134,18 @@ int pc_set_relaxed(pc_handle* h, int relaxed);
  * multiple of k buffer_size frames.
  */
 int pc_set_step_blocks(pc_handle* h, int k);
+
+/*
+ * Kernel tile shape, no reference counterpart (the measured-GPU autotuner,
+ * partconv_gb300/autotune.py, picks it the way the reference's tune.py picks
+ * layouts, src/tune.py:21-154): the streaming FDL multiply-accumulate of the
+ * parts a fire does not sum itself is cut into spread tasks of spread_bins
+ * bins (64, 128, 256 or 512) and spread_parts parts (1..64; a level
+ * keeps one partial-sum row per group of spread_parts parts).  0 keeps the
+ * default (128 bins, 16 parts).  Call before setup; results differ between
+ * tile shapes only by float32 rounding (sums grouped differently).
+ */
+int pc_set_tiles(pc_handle* h, int spread_bins, int spread_parts);
 
 /*
  * PartConvMulti::run(output, input, frameCount) -- src/partconvMulti.h:60,

@@ -43,6 +43,8 @@ class PCInfo(C.Structure):
         ("frame_num", C.c_longlong),
         ("device_bytes", C.c_longlong),
         ("step_blocks", C.c_int),
+        ("spread_bins", C.c_int),
+        ("spread_parts", C.c_int),
     ]
 
 
@@ -77,6 +79,7 @@ SIGNATURES = {
                                   C.POINTER(_f32p), _i32p, _i32p, _i32p, _f32p, _i32p]),
     "pc_set_relaxed": (C.c_int, [C.c_void_p, C.c_int]),
     "pc_set_step_blocks": (C.c_int, [C.c_void_p, C.c_int]),
+    "pc_set_tiles": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "pc_run": (C.c_int, [C.c_void_p, _f32p, _f32p, C.c_int]),
     "pc_process": (C.c_int, [C.c_void_p, _f32p, _f32p, C.c_longlong, C.c_int]),
     "pc_process_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),

@@ -6,9 +6,11 @@ searches a cost model (4k log2(2N) + 4 per block).  Here candidates are
 timed on the GPU engine itself: each candidate layout runs a batch of
 identical streams (the way the batched engine will run it) for a few
 hyperperiods of base steps, and the layout with the lowest time per
-stream-step wins.  Results are cached per (IR length class, base block,
-batch class, GPU) in a JSON file, the analogue of the reference's FFTW
-wisdom file (src/partconvMulti.cpp:250-254).
+stream-step wins.  The kernel tile shape (bins and parts per spread task,
+pc_set_tiles) is then measured the same way for the winning layout, and for
+a whole mixed workload by choose_tiles.  Results are cached per (IR length
+class, base block, batch class, GPU) in a JSON file, the analogue of the
+reference's FFTW wisdom file (src/partconvMulti.cpp:250-254).
 """
 from __future__ import annotations
 
@@ -25,7 +27,14 @@ DEFAULT_CACHE = os.environ.get("PARTCONV_AUTOTUNE_CACHE") or os.path.join(
 _lock = threading.Lock()
 
 
-def candidate_layouts(ir_len: int, N0: int, max_block: int = 16384):
+MAX_BLOCK = 65536   # the engine's PC_MAX_BLOCK (blocks above 16384 run on 8-CTA clusters)
+
+# (bins, parts) per spread task tried for a layout or a workload
+TILE_CANDIDATES = [(64, 16), (128, 8), (128, 16), (128, 32), (256, 16), (256, 32), (512, 32)]
+DEFAULT_TILES = (128, 16)
+
+
+def candidate_layouts(ir_len: int, N0: int, max_block: int = MAX_BLOCK):
     """Level chains with ratios 2, 4, 8 and 16 and largest blocks up to
     max_block, each with minimum slack (every level fires within its step)
     and with the reference's strict slack (larger levels' fires run beside
@@ -68,19 +77,28 @@ def _len_class(ir_len: int) -> int:
     return 1 << int(np.ceil(np.log2(max(ir_len, 2))))
 
 
-def measure_layout(N, P, ir_len: int, batch: int = 32, steps: int = 0, seed: int = 0, step_blocks: int = 1) -> float:
+def measure_layout(N, P, ir_len: int, batch: int = 32, steps: int = 0, seed: int = 0, step_blocks: int = 1,
+                   tiles=None) -> float:
     """Device time (µs) per base step of `batch` streams of this layout
-    (step_blocks: base blocks per launch, pc_set_step_blocks)."""
+    (step_blocks: base blocks per launch, pc_set_step_blocks; tiles: (bins,
+    parts) per spread task, pc_set_tiles)."""
+    rng = np.random.default_rng(seed)
+    N0 = N[0]
+    pcs = [dict(ir=wl.decaying_ir(rng, ir_len, 1.0), N=N, P=P, in_ch=s, out_ch=s) for s in range(batch)]
+    return measure_pcs(pcs, N0, steps=steps, step_blocks=step_blocks, tiles=tiles)
+
+
+def measure_pcs(pcs, N0: int, steps: int = 0, step_blocks: int = 1, tiles=None) -> float:
+    """Device time (µs) per base step of one handle holding these PCs (one
+    stream each), over at least two hyperperiods."""
     import torch
 
     from .multi import PartConvMulti
     from . import PC_PLANAR
 
-    rng = np.random.default_rng(seed)
-    N0 = N[0]
-    pcs = [dict(ir=wl.decaying_ir(rng, ir_len, 1.0), N=N, P=P, in_ch=s, out_ch=s) for s in range(batch)]
-    m = PartConvMulti(step_blocks=step_blocks)
-    m.setup_layout(48000, N0, batch, batch, pcs)
+    batch = len(pcs)
+    m = PartConvMulti(step_blocks=step_blocks, tiles=tiles)
+    m.setup_layout(48000, N0, batch, batch, [p | dict(in_ch=s, out_ch=s) for s, p in enumerate(pcs)])
     H = max(m.info().hyperperiod, m.info().step_blocks)
     nsteps = steps or max(2 * H, 128)
     nsteps = (nsteps + H - 1) // H * H
@@ -126,6 +144,16 @@ def _key(ir_len, N0, batch, gpu=None):
     return f"{gpu or _gpu_name()}|N0={N0}|len={lc}|batch={bc}", lc, bc
 
 
+def _save(cache, key, rec):
+    with _lock:
+        cur = _load(cache)
+        cur[key] = rec
+        tmp = cache + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(cur, f, indent=1, sort_keys=True)
+        os.replace(tmp, cache)
+
+
 def cached_layout(ir_len: int, N0: int, batch: int = 32, cache: str | None = DEFAULT_CACHE):
     """The cached choice for this key without measuring (None on a miss).
     Without a GPU (or with no entry for this one) an entry of the same
@@ -147,24 +175,70 @@ def choose_layout(ir_len: int, N0: int, batch: int = 32, cache: str | None = DEF
     key, lc, bc = _key(ir_len, N0, batch)
     with _lock:
         db = _load(cache) if cache else {}
-    if key not in db:
+    if key not in db or "tiles" not in db[key]["best"]:
         results = []
         for N, P in candidate_layouts(lc, N0):
             us = measure_layout(N, P, lc, batch=bc)
             results.append({"N": N, "P": P, "us_per_step": us})
             if verbose:
                 print(f"  {N} {P}: {us:.2f} us/step")
-        best = min(results, key=lambda r: r["us_per_step"])
-        db[key] = {"best": best, "candidates": results}
+        best = dict(min(results, key=lambda r: r["us_per_step"]))
+        # the kernel tile shape, measured on the winning layout
+        tiles = []
+        for tb, tp in TILE_CANDIDATES:
+            us = measure_layout(best["N"], best["P"], lc, batch=bc, tiles=(tb, tp))
+            tiles.append({"tiles": [tb, tp], "us_per_step": us})
+            if verbose:
+                print(f"  tiles {tb}x{tp}: {us:.2f} us/step")
+        bt = min(tiles, key=lambda r: r["us_per_step"])
+        best["tiles"] = bt["tiles"]
+        best["us_per_step_tiled"] = bt["us_per_step"]
+        db[key] = {"best": best, "candidates": results, "tile_candidates": tiles}
         if cache:
-            with _lock:
-                cur = _load(cache)
-                cur[key] = db[key]
-                tmp = cache + ".tmp"
-                with open(tmp, "w") as f:
-                    json.dump(cur, f, indent=1, sort_keys=True)
-                os.replace(tmp, cache)
+            _save(cache, key, db[key])
     return _fit(db[key]["best"]["N"], db[key]["best"]["P"], ir_len)
+
+
+def cached_tiles(ir_len: int, N0: int, batch: int = 32, cache: str | None = DEFAULT_CACHE):
+    """The tile shape cached with this length class's layout (None: none)."""
+    if not cache:
+        return None
+    db = _load(cache)
+    key, _, _ = _key(ir_len, N0, batch)
+    rec = db.get(key)
+    if rec is None:
+        tail = key[key.index("|"):]
+        rec = next((v for k, v in sorted(db.items()) if k.endswith(tail)), None)
+    t = rec["best"].get("tiles") if rec else None
+    return tuple(t) if t else None
+
+
+def choose_tiles(pcs, N0: int, name: str, cache: str | None = DEFAULT_CACHE, measure: bool = True,
+                 verbose: bool = False):
+    """Tile shape (bins, parts per spread task) for one handle holding these
+    PCs, measured on the handle itself for every TILE_CANDIDATES entry and
+    cached under `name` (a workload with layouts of several length classes
+    takes one shape per handle).  Without measuring, a miss gives None."""
+    key = f"{_gpu_name()}|tiles|{name}|N0={N0}|pcs={len(pcs)}"
+    with _lock:
+        db = _load(cache) if cache else {}
+    rec = db.get(key)
+    if rec is None and not measure:
+        tail = key[key.index("|"):]
+        rec = next((v for k, v in sorted(db.items()) if k.endswith(tail)), None)
+    if rec is None:
+        if not measure:
+            return None
+        res = []
+        for tb, tp in TILE_CANDIDATES:
+            us = measure_pcs(pcs, N0, tiles=(tb, tp))
+            res.append({"tiles": [tb, tp], "us_per_step": us})
+            if verbose:
+                print(f"  tiles {tb}x{tp}: {us:.2f} us/step")
+        rec = {"best": dict(min(res, key=lambda r: r["us_per_step"])), "candidates": res}
+        if cache:
+            _save(cache, key, rec)
+    return tuple(rec["best"]["tiles"])
 
 
 # ---------------------------------------------------------------------------
@@ -178,7 +252,7 @@ def model_level_cost(N: int, P: int, N0: int, k: float = 1.5) -> float:
     return (4.0 * k * np.log2(2 * N) + 4.0 * P) * N0 / N
 
 
-def optimal_part(ir_len: int, N0: int, level_cost=None, max_block: int = 16384, strict: bool = False):
+def optimal_part(ir_len: int, N0: int, level_cost=None, max_block: int = MAX_BLOCK, strict: bool = False):
     """Layout (N, P) minimising the sum of level_cost(N, P, N0) over levels.
 
     Levels have power-of-two blocks growing from N0 (any factor), and each
@@ -259,3 +333,41 @@ def measured_level_costs(N0: int, sizes=None, parts=(2, 8), trials: int = 200):
         a, b = fit[N]
         return (a + b * P) * n0 / N
     return cost
+
+
+def retune_batched_workload(streams: int = 32, samples: int = 1 << 19, cache: str | None = DEFAULT_CACHE,
+                            verbose: bool = True):
+    """Measure and cache the batched 32-stream workload's choices: a layout
+    (and tile shape) per IR length class, then one tile shape for the handle
+    holding all streams.  Existing entries for this GPU are measured again."""
+    if cache:
+        db = _load(cache)
+        gpu = _gpu_name()
+        for k in [k for k in db if k.startswith(gpu + "|")]:
+            del db[k]
+        with _lock:
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(db, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+
+    def pick(L, n0):
+        if verbose:
+            print(f"IR length {L} (class {_len_class(L)}):")
+        return choose_layout(L, n0, batch=streams, cache=cache, verbose=verbose)
+
+    c = wl.cfg2(n_streams=streams, n_samples=1024, layout_fn=pick)
+    pcs = [dict(ir=h, N=N, P=P) for h, (N, P) in zip(c["irs"], c["layouts"])]
+    if verbose:
+        print("tile shape of the whole handle:")
+    return choose_tiles(pcs, c["N0"], "cfg2", cache=cache, verbose=verbose)
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="measure and cache layouts and tile shapes on this GPU")
+    ap.add_argument("--cache", default=DEFAULT_CACHE)
+    ap.add_argument("--streams", type=int, default=32)
+    a = ap.parse_args()
+    print("tiles:", retune_batched_workload(a.streams, cache=a.cache))

@@ -155,6 +155,8 @@ struct pc_handle {
     int H = 1;        // hyperperiod (base steps)
     int G = 64;       // base steps per captured graph (multiple of H and KB)
     int req_kb = 1;   // base blocks per step requested (pc_set_step_blocks)
+    int req_tile_bins = 0, req_tile_parts = 0;   // spread tile shape requested (pc_set_tiles; 0: default)
+    int TB = 0, TP = 0;                          // spread tile shape in use: bins and parts per task
     int KB = 1;       // base blocks per step in use: a launch computes KB level-0 blocks
     int Hs = 1;       // task-table phases: steps (of KB base blocks) per hyperperiod
     int maxN = 0;
@@ -452,6 +454,11 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             while (KB > 1 && (p.N[L] / N0) % KB) KB >>= 1;
     h->KB = KB;
     h->Hs = std::max(1, Hh / KB);
+    // spread tile shape: bins and parts per spread task
+    const int TB = h->req_tile_bins > 0 ? h->req_tile_bins : spread_task_bins();
+    const int TP = h->req_tile_parts > 0 ? h->req_tile_parts : spread_task_parts();
+    h->TB = TB;
+    h->TP = TP;
     // parts a K-block level-0 fire sums itself; spread rows take the rest
     const int QC = KB > 1 ? multi_fire_parts(N0, KB) : 2;
     h->G = std::max(h->G, KB);
@@ -581,7 +588,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 {   // spread tasks sum parts >= 2 KB (level 0), >= 2 (deferred levels) or >= 1
                     const int p_lo = L == 0 ? (KB > 1 ? std::min(p.P[L], QC) : 2) : (dfl[li] ? 2 : 1);
                     const int np = p.P[L] - p_lo;
-                    l.npart = np > 0 ? (np + spread_task_parts() - 1) / spread_task_parts() : 1;
+                    l.npart = np > 0 ? (np + TP - 1) / TP : 1;
                 }
                 s += (long)p.N[L] * p.P[L];
             }
@@ -679,8 +686,8 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                 hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
                 p_lo = 1;
             }
-            for (int k0 = lo; k0 < hi; k0 += spread_task_bins())
-                for (int r = 0; r < l.npart; ++r) {   // parts [p_lo + 16 r, p_lo + 16 (r + 1)) into row r
+            for (int k0 = lo; k0 < hi; k0 += TB)
+                for (int r = 0; r < l.npart; ++r) {   // parts [p_lo + TP r, p_lo + TP (r + 1)) into row r
                     Task t{};
                     t.kind = 1;
                     t.N = l.N;
@@ -688,10 +695,11 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                     t.T = l.T;
                     t.s_blocks = l.s_blocks;
                     t.cs = l.cs;
+                    t.M = TB;   // bins per task
                     t.k0 = k0;
-                    t.k1 = std::min(hi, k0 + spread_task_bins());
-                    t.p_lo = p_lo + r * spread_task_parts();
-                    t.in_ch = std::min(l.P, p_lo + (r + 1) * spread_task_parts());
+                    t.k1 = std::min(hi, k0 + TB);
+                    t.p_lo = p_lo + r * TP;
+                    t.in_ch = std::min(l.P, p_lo + (r + 1) * TP);
                     t.out_ch = r;
                     t.lv_index = li;
                     t.dfer = dwin[li] > 0;
@@ -764,10 +772,12 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
         const int sc = h->l0_class;
         for (int li = 0; li < nlv; ++li) {
             const DevLevel& l = h->h_lv[li];
+            // level 0's K-block spreads (spread_multi) keep the default tile width
+            const int tb = l.T == 1 ? spread_task_bins() : TB;
             auto add_spreads = [&](int lo, int hi, int p_lo, long long origin, std::vector<Task>& dst, double& bytes,
                                    double blocks) {
-                for (int k0 = lo; k0 < hi; k0 += spread_task_bins())
-                    for (int q = 0; q < l.npart; ++q) {   // parts [p_lo + 16 q, p_lo + 16 (q + 1)) into row q
+                for (int k0 = lo; k0 < hi; k0 += tb)
+                    for (int q = 0; q < l.npart; ++q) {   // parts [p_lo + TP q, p_lo + TP (q + 1)) into row q
                         Task t{};
                         t.kind = 1;
                         t.N = l.N;
@@ -775,10 +785,11 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                         t.T = l.T;
                         t.s_blocks = l.s_blocks;
                         t.cs = l.cs;
+                        t.M = tb;   // bins per task
                         t.k0 = k0;
-                        t.k1 = std::min(hi, k0 + spread_task_bins());
-                        t.p_lo = p_lo + q * spread_task_parts();
-                        t.in_ch = std::min(l.P, p_lo + (q + 1) * spread_task_parts());
+                        t.k1 = std::min(hi, k0 + tb);
+                        t.p_lo = p_lo + q * TP;
+                        t.in_ch = std::min(l.P, p_lo + (q + 1) * TP);
                         t.out_ch = q;
                         t.lv_index = li;
                         t.dfer = l.T > 1;
@@ -968,6 +979,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
     h->bank.wlog = kWlog;
     h->bank.N0 = N0;
     h->bank.kb = KB;
+    h->bank.tb = TB;
     h->bank.kq = 0;
     for (auto& p : h->specs) h->bank.kq = std::max(h->bank.kq, std::min(p.P[0], QC));
     h->bank.n_out = n_out;
@@ -1276,6 +1288,17 @@ int pc_set_step_blocks(pc_handle* h, int k) {
     return PC_OK;
 }
 
+int pc_set_tiles(pc_handle* h, int spread_bins, int spread_parts) {
+    if (!h) return PC_ERR_ARG;
+    if (h->ready) return fail(h, PC_ERR_STATE, "tile shapes must be set before setup");
+    if (spread_bins != 0 && !spread_bins_ok(spread_bins))
+        return fail(h, PC_ERR_ARG, "bins per spread task must be 64, 128, 256 or 512 (or 0)");
+    if (spread_parts < 0 || spread_parts > 64) return fail(h, PC_ERR_ARG, "parts per spread task must be in [1, 64] (or 0)");
+    h->req_tile_bins = spread_bins;
+    h->req_tile_parts = spread_parts;
+    return PC_OK;
+}
+
 int pc_set_relaxed(pc_handle* h, int relaxed) {
     if (!h) return PC_ERR_ARG;
     h->relaxed = relaxed ? 1 : 0;
@@ -1432,6 +1455,8 @@ int pc_get_info(const pc_handle* h, pc_info* info) {
     info->relaxed = h->relaxed;
     info->hyperperiod = h->H;
     info->step_blocks = h->KB;
+    info->spread_bins = h->TB;
+    info->spread_parts = h->TP;
     info->frame_num = h->frame_num;
     info->device_bytes =
         (long long)h->arena_bytes + (long long)sizeof(float) * (h->big_in_cap + h->big_out_cap + h->rtmp_cap);

@@ -31,7 +31,7 @@ struct DevLevel {
     int cs;         // row stride in complex values (N_L + 2)
     int rmask;      // output ring size - 1 (levels >= 1)
     int pc;         // owning PC
-    int npart;      // partial-sum rows (spread tasks cover at most kSpreadParts parts each)
+    int npart;      // partial-sum rows (a spread task covers at most the handle's parts per task)
     float2* H;      // [P][cs]
     float2* X;      // [P][cs]
     float2* Yp;     // [npart][2][cs]: row q, block parity ([npart][2K][cs], block mod 2K, for
@@ -60,7 +60,8 @@ struct DevPC {
 // inverse FFT, output (level 0 also emits the step's output); k0 holds the
 // number of partial-sum rows to add (0 means 1).  kind 1 (spread): partial
 // FDL MAC over bins [k0, k1) and parts [p_lo, in_ch) (in_ch 0: up to P) of
-// a level's next block, written to partial-sum row out_ch.
+// a level's next block, written to partial-sum row out_ch; a spread task
+// keeps its bins per task (the tile width) in M (0: the default).
 struct Task {
     int kind, N, logN, P;
     int T, s_blocks, cs, rmask;
@@ -119,6 +120,7 @@ struct Bank {
     int n_out;
     int kb;                // base blocks per step (level-0 sub-blocks of one fire); 0 or 1: one
     int kq;                // with kb > 1: most parts a level-0 fire sums itself (shared-memory size)
+    int tb;                // bins per spread task of the handle's step kernels (0: the default)
     // per output channel mixing lists (mix_mode 2): out_off[o]..out_off[o+1]
     const int* out_off;
     const int* out_pcs;

@@ -28,8 +28,11 @@ constexpr int kClusterMaxN = 65536;      // largest block of class 3
 // threads per CTA of a class
 int class_threads(int cls);
 // bins one spread task covers
+// default bins and parts per spread task (the tile shape pc_set_tiles overrides)
 int spread_task_bins();
 int spread_task_parts();
+// bins per spread task the spread kernels accept (64, 128, 256 or 512)
+bool spread_bins_ok(int bins);
 size_t class_smem_bytes(int cls, int maxN);
 // dynamic shared memory of a step launch (class, largest block, the bank's
 // base blocks per step)

@@ -89,19 +89,32 @@ __host__ __device__ constexpr size_t fire_smem_bytes(int N, bool prefetch) {
 }
 
 // ---------------------------------------------------------------------------
-// Spread: NT threads = G part-groups x 64 threads; a thread owns two bins,
-// group g sums parts p_lo + g, p_lo + g + G, ...; groups are added in order.
+// Spread: the streaming FDL MAC over the task's bins [k0, k1) and parts
+// [p_lo, p_hi).  NT threads form G = NT / LANES part-groups of LANES
+// threads; thread t owns bins k0 + 2 (t mod LANES), +1 (one float4) and sums
+// parts p_lo + g, + G, ... (g = t / LANES); the groups are added in order
+// through shared memory.  Bins per task (2 LANES; a tile shape the autotuner
+// picks per handle) travel in the task's M field, 0 meaning kSpreadBins;
+// each width is its own instantiation (constant strides): the step kernel
+// is instantiated per width and launched for the handle's width.  Parts per task
+// set how many partial-sum rows a level keeps.
+//
+// Measured and rejected: the G threads of one bin pair as adjacent lanes of
+// a warp, summed by warp shuffles instead of shared memory (no barrier) --
+// 33 % slower per step on 32 streams (3.48 -> 4.65 us for 256x14 | 2048x14 |
+// 16384x15): each warp load then spans G rows instead of one.  A runtime
+// group width in the same loop cost 4 % (3.48 -> 3.63 us).
 // ---------------------------------------------------------------------------
-constexpr int kSpreadLanes = 64;   // threads per part-group: a task covers 128 bins
-// parts per spread task: one round of loads (4 groups x 4 in flight) per CTA
-constexpr int kSpreadParts = 16;
+constexpr int kSpreadBins = 128;   // default bins per task
+constexpr int kSpreadParts = 16;   // default parts per task (one round of loads per thread)
+constexpr int kSpreadLanes = 64;   // K-block level-0 spreads (spread_multi): threads per part-group
 
 // kb: base blocks per step (level 0 keeps 2 kb partial-sum buffers per row).
-template <int NT>
-__device__ __forceinline__ void spread_body(const Task& tk, long long c, float4* red, int kb) {
-    constexpr int G = NT / kSpreadLanes;
-    const int lane = threadIdx.x % kSpreadLanes;
-    const int g = threadIdx.x / kSpreadLanes;
+template <int NT, int LANES>
+__device__ __forceinline__ void spread_lanes(const Task& tk, long long c, float4* red, int kb) {
+    constexpr int G = NT / LANES;
+    const int lane = threadIdx.x % LANES;
+    const int g = threadIdx.x / LANES;
     const int k = tk.k0 + 2 * lane;
     const bool active = k < tk.k1;
     long long bt;      // block whose partial sum this step builds
@@ -147,15 +160,26 @@ __device__ __forceinline__ void spread_body(const Task& tk, long long c, float4*
         }
     }
     if (G > 1) {
-        if (g > 0) red[(g - 1) * kSpreadLanes + lane] = acc;
+        if (g > 0) red[(g - 1) * LANES + lane] = acc;
         __syncthreads();
         if (g == 0 && active) {
 #pragma unroll
-            for (int j = 1; j < G; ++j) acc = f4add(acc, red[(j - 1) * kSpreadLanes + lane]);
+            for (int j = 1; j < G; ++j) acc = f4add(acc, red[(j - 1) * LANES + lane]);
             *reinterpret_cast<float4*>(dst + k) = acc;
         }
     } else if (active) {
         *reinterpret_cast<float4*>(dst + k) = acc;
+    }
+}
+
+// red: NT - 32 float4 of shared memory at least
+template <int NT>
+__device__ __forceinline__ void spread_body(const Task& tk, long long c, float4* red, int kb) {
+    switch (tk.M > 0 ? tk.M : kSpreadBins) {
+        case 64: spread_lanes<NT, 32>(tk, c, red, kb); break;
+        case 256: spread_lanes<NT, (NT >= 128 ? 128 : NT)>(tk, c, red, kb); break;
+        case 512: spread_lanes<NT, (NT >= 256 ? 256 : NT)>(tk, c, red, kb); break;
+        default: spread_lanes<NT, 64>(tk, c, red, kb); break;
     }
 }
 
@@ -993,7 +1017,9 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
 // ---------------------------------------------------------------------------
 // MULTI: the bank runs several base blocks per step (level-0 fires take
 // fire_multi); a separate instance so the one-block kernel keeps its registers.
-template <class C, bool MULTI = false>
+// LANES: threads per spread part-group (bins per spread task / 2), the tile
+// width of the handle, one instance per width.
+template <class C, bool MULTI = false, int LANES = 64>
 __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __restrict__ tasks, RunState rs_val,
                                                      const RunState* rs_dev, int step_in_batch) {
     extern __shared__ float4 dyn_smem[];
@@ -1023,7 +1049,7 @@ __global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __re
                 return;
             }
         }
-        spread_body<C::NT>(tk, c, dyn_smem, kb);
+        spread_lanes<C::NT, (LANES < C::NT ? LANES : C::NT)>(tk, c, dyn_smem, kb);
         return;
     }
     if constexpr (MULTI && C::PREFETCH) {
@@ -1080,13 +1106,14 @@ __global__ void __launch_bounds__(C::NT) pool_kernel(Bank bank, const Task* __re
         hi = (j == nch - 1) ? tk.cs : (int)(((long long)(j + 1) * tk.cs / nch) & ~1LL);
         p_lo = 1;
     }
-    const int k0 = lo + (pm.sub - 1) * (2 * kSpreadLanes);
+    const int k0 = lo + (pm.sub - 1) * kSpreadBins;
     if (k0 >= hi) return;
     __syncthreads();   // everyone has read the fire form of the record
     if (tid == 0) {
         tk.kind = 1;
         tk.k0 = k0;
-        tk.k1 = min(hi, k0 + 2 * kSpreadLanes);
+        tk.k1 = min(hi, k0 + kSpreadBins);
+        tk.M = 0;        // default bins per task
         tk.p_lo = p_lo;
         tk.in_ch = 0;    // all parts from p_lo
         tk.out_ch = 0;   // partial-sum row 0
@@ -1149,7 +1176,7 @@ __global__ void __launch_bounds__(NT) spectra_kernel(const SpectraJob* __restric
 constexpr int kSideNT = 256;
 __global__ void __launch_bounds__(kSideNT) spread_kernel(const Task* __restrict__ tasks, RunState rs_val,
                                                         const RunState* rs_dev, int step_in_batch) {
-    __shared__ float4 red[(kSideNT / kSpreadLanes - 1) * kSpreadLanes];
+    __shared__ float4 red[kSideNT];
     __shared__ __align__(16) Task tk;
     __shared__ long long step_base;
     const int tid = threadIdx.x;
@@ -1177,8 +1204,9 @@ static_assert(Cls2::MAXN == kMaxBlockOneCta, "class 2 is the largest one-CTA cla
 static const int kNT[3] = {Cls0::NT, Cls1::NT, Cls2::NT};
 static const bool kPrefetch[3] = {Cls0::PREFETCH, Cls1::PREFETCH, Cls2::PREFETCH};
 int class_threads(int cls) { return cls == 3 ? 512 : kNT[cls]; }
-int spread_task_bins() { return 2 * kSpreadLanes; }
+int spread_task_bins() { return kSpreadBins; }
 int spread_task_parts() { return kSpreadParts; }
+bool spread_bins_ok(int bins) { return bins == 64 || bins == 128 || bins == 256 || bins == 512; }
 
 size_t class_smem_bytes(int cls, int maxN) {
     if (cls == 3) return cluster_smem_bytes();
@@ -1212,9 +1240,11 @@ cudaError_t prepare_kernels() {
     size_t s0 = class_smem_bytes(0, Cls0::MAXN);
     for (int N = 16; N <= Cls0::MAXN; N *= 2)
         for (int k = 2; k <= max_step_blocks(N); k *= 2) s0 = std::max(s0, multi_smem_bytes(N, k, multi_fire_parts(N, k)));
-    e = cudaFuncSetAttribute(step_kernel<Cls0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)class_smem_bytes(0, Cls0::MAXN));
-    if (e != cudaSuccess) return e;
+    for (auto fn : {step_kernel<Cls0>, step_kernel<Cls0, false, 32>, step_kernel<Cls0, false, 128>,
+                    step_kernel<Cls0, false, 256>}) {
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)class_smem_bytes(0, Cls0::MAXN));
+        if (e != cudaSuccess) return e;
+    }
     e = cudaFuncSetAttribute(step_kernel<Cls0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s0);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(step_kernel<Cls1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1273,7 +1303,12 @@ cudaError_t launch_step_class(int cls, int grid, int maxN, const Bank& bank, con
     switch (cls) {
         case 0:
             if (bank.kb > 1) return cudaLaunchKernelEx(&cfg, step_kernel<Cls0, true>, bank, tasks, rs, rs_dev, step_in_batch);
-            return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
+            switch (bank.tb) {   // the handle's spread tile width
+                case 64: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0, false, 32>, bank, tasks, rs, rs_dev, step_in_batch);
+                case 256: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0, false, 128>, bank, tasks, rs, rs_dev, step_in_batch);
+                case 512: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0, false, 256>, bank, tasks, rs, rs_dev, step_in_batch);
+                default: return cudaLaunchKernelEx(&cfg, step_kernel<Cls0>, bank, tasks, rs, rs_dev, step_in_batch);
+            }
         case 1: return cudaLaunchKernelEx(&cfg, step_kernel<Cls1>, bank, tasks, rs, rs_dev, step_in_batch);
         default: return cudaLaunchKernelEx(&cfg, step_kernel<Cls2>, bank, tasks, rs, rs_dev, step_in_batch);
     }

@@ -54,10 +54,12 @@ def _i32(a) -> np.ndarray:
 class PartConvMulti:
     relaxed = 0
 
-    def __init__(self, verbosity: int = 0, step_blocks: int = 1):
+    def __init__(self, verbosity: int = 0, step_blocks: int = 1, tiles=None):
         """step_blocks > 1: offline throughput mode, `step_blocks` base blocks
         per step (pc_set_step_blocks); run() is then unavailable and process()
-        wants a multiple of step_blocks * buffer_size frames."""
+        wants a multiple of step_blocks * buffer_size frames.
+        tiles: (bins, parts) per spread task (pc_set_tiles), e.g. the
+        autotuner's choice; None keeps the default."""
         self.verbosity = verbosity
         self._lib = nat.lib()
         self._h = self._lib.pc_create(int(verbosity))
@@ -65,6 +67,8 @@ class PartConvMulti:
             raise PartConvError(nat.PC_ERR_NOMEM, "pc_create failed")
         if step_blocks != 1:
             nat.check(self._h, self._lib.pc_set_step_blocks(self._h, int(step_blocks)))
+        if tiles:
+            nat.check(self._h, self._lib.pc_set_tiles(self._h, int(tiles[0]), int(tiles[1])))
         self.FS = 0
         self.buffer_size = 0
         self.max_block_size = 0

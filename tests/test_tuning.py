@@ -121,24 +121,42 @@ def test_cached_layout_lookup_and_fit(tmp_path):
 
 
 def test_shipped_cache_is_consistent():
-    """The cache shipped with the package: every key names a GPU, base block,
-    length class and batch class; its best layout is the fastest measured
-    candidate, and every stored layout is valid for its length class."""
+    """The cache shipped with the package.  Layout entries: every key names a
+    GPU, base block, length class and batch class; the best layout is the
+    fastest measured candidate, every stored layout is valid for its length
+    class, and the entry carries the tile shape measured for it (the fastest
+    tile candidate).  Workload tile entries: the best shape is the fastest
+    candidate and every candidate is a shape the engine accepts."""
     import re
 
     with open(autotune.DEFAULT_CACHE) as f:
         db = json.load(f)
     assert db
+    n_layout = n_tiles = 0
     for key, rec in db.items():
+        t = re.fullmatch(r"(.+)\|tiles\|(.+)\|N0=(\d+)\|pcs=(\d+)", key)
+        if t:
+            n_tiles += 1
+            cands = rec["candidates"]
+            assert rec["best"]["us_per_step"] == min(c["us_per_step"] for c in cands)
+            for c in cands:
+                b, p = c["tiles"]
+                assert b in (64, 128, 256, 512) and 1 <= p <= 64 and c["us_per_step"] > 0
+            continue
         m = re.fullmatch(r"(.+)\|N0=(\d+)\|len=(\d+)\|batch=(\d+)", key)
         assert m, key
+        n_layout += 1
         n0, lc = int(m.group(2)), int(m.group(3))
         assert lc & (lc - 1) == 0
         best = rec["best"]
         cands = rec["candidates"]
-        assert cands and best in cands
+        assert {k: best[k] for k in ("N", "P", "us_per_step")} in cands
         assert best["us_per_step"] == min(c["us_per_step"] for c in cands)
         for c in cands:
             assert c["N"][0] == n0 and c["us_per_step"] > 0
             st, _, _, msg = check_layout(c["N"], c["P"], lc)
             assert st == 0, (key, c, msg)
+        tc = rec["tile_candidates"]
+        assert list(best["tiles"]) == min(tc, key=lambda r: r["us_per_step"])["tiles"]
+        assert {tuple(r["tiles"]) for r in tc} == set(autotune.TILE_CANDIDATES)
+    assert n_layout >= 5 and n_tiles >= 1

@@ -54,6 +54,10 @@ def parse_args():
                     help="cfg2: base blocks per step (pc_set_step_blocks); 1 = one launch per 256-sample block "
                          "(the headline). The other mode (4, or 1) is measured beside it")
     ap.add_argument("--no-alt", action="store_true", help="cfg2: skip the other blocks-per-step mode")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="cfg2: skip the other workloads' legs (cfg3 MIMO, cfg4 adjoint, cfg5 serving) that the "
+                         "default run records beside the headline")
+    ap.add_argument("--serve-seconds", type=float, default=40.0, help="cfg5 leg: real-time limit of the load run")
     ap.add_argument("--layouts", default="auto", choices=["auto", "chain"],
                     help="cfg2 layouts: measured-GPU autotuner (cached) or the minimum-slack chain")
     ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"],
@@ -506,6 +510,21 @@ def run_ours(args):
             line["parity"] = parity
         if clk:
             line["clocks"] = clk
+        if not args.no_legs and ws == 1:
+            # the other workloads, each its own measurement on this GPU, so one
+            # default run records them beside the headline
+            import argparse as _ap
+
+            legs = {}
+            for name, fn, steps in (("cfg3_mimo", run_mimo, 5), ("cfg4_adjoint", run_adjoint, 20),
+                                    ("cfg5_serving", run_serving, 0)):
+                sub = _ap.Namespace(**vars(args))
+                sub.steps, sub.warmup, sub.samples, sub.streams = max(steps, 1), 3, None, 32
+                try:
+                    legs[name] = fn(sub)
+                except Exception as e:   # a leg that fails is reported, the headline stands
+                    legs[name] = {"error": f"{type(e).__name__}: {e}"}
+            line["legs"] = legs
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -576,8 +595,7 @@ def run_mimo(args):
     }
     if clk:
         line["clocks"] = clk
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 def run_adjoint(args):
@@ -652,7 +670,7 @@ def run_adjoint(args):
     e1.record(stream)
     torch.cuda.synchronize()
     dense_ms = e0.elapsed_time(e1) / args.steps
-    print(json.dumps({"metric": "audio-s/s (differentiable conv, forward + backward)", "value": audio / (ms / 1e3),
+    return ({"metric": "audio-s/s (differentiable conv, forward + backward)", "value": audio / (ms / 1e3),
                       "unit": "audio-s/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
                       "data": "synthetic (seeded numpy PCG64, cfg seed 1004)",
@@ -666,8 +684,7 @@ def run_adjoint(args):
                                         "float64; fd64: FP64 central differences, step 1e-3, 64 random IR taps "
                                         "and 64 random input samples"},
                       "dense_torch_fft_fp32": {"ms_per_step": dense_ms, "value": audio / (dense_ms / 1e3),
-                                               "unit": "audio-s/s"}}))
-    return 0
+                                               "unit": "audio-s/s"}})
 
 
 def run_plain_mono(args):
@@ -762,14 +779,13 @@ def run_serving(args):
     noise = (0.1 * np.random.default_rng(5).standard_normal(1 << 22)).astype(np.float32)
     gen_s = time.time() - t0
     srv = Server(hbm_budget_bytes=160 << 30, max_pcs_per_pool=4096)
-    stats = srv.run_load(reqs, irs, noise, max_concurrent=1000, max_seconds=120.0)
-    print(json.dumps({"metric": "serving: per-block latency and audio-s/s (cfg5 mix, real time)",
+    stats = srv.run_load(reqs, irs, noise, max_concurrent=1000, max_seconds=args.serve_seconds)
+    return ({"metric": "serving: per-block latency and audio-s/s (cfg5 mix, real time)",
                       "value": stats["audio_s_per_s"], "unit": "audio-s/s", "n_gpus": 1, "higher_is_better": True,
                       "dtype": "f32", "data": "synthetic (seeded; inputs are slices of one noise buffer)",
                       "config": {"workload": "cfg5: 1000 streams, Poisson 200/s, 1/2/8 ch, IR 2^12..2^20, "
                                              "N0 64..1024, 10 s each", "request_gen_s": gen_s},
-                      "serving": stats}))
-    return 0
+                      "serving": stats})
 
 
 def main():
@@ -780,12 +796,10 @@ def main():
         return run_reference(args)
     if args.workload == "cfg1":
         return run_plain_mono(args)
-    if args.workload == "cfg3":
-        return run_mimo(args)
-    if args.workload == "cfg4":
-        return run_adjoint(args)
-    if args.workload == "cfg5":
-        return run_serving(args)
+    if args.workload in ("cfg3", "cfg4", "cfg5"):
+        line = {"cfg3": run_mimo, "cfg4": run_adjoint, "cfg5": run_serving}[args.workload](args)
+        print(json.dumps(line))
+        return 0
     return run_ours(args)
 
 

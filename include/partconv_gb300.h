@@ -388,6 +388,44 @@ long long pcs_kernel_launches(const pcs_handle* h);
 const char* pcs_last_error(const pcs_handle* h);
 void pcs_destroy(pcs_handle* h);
 
+/* Most pools pcs_run_load drives. */
+#define PCS_LOAD_MAX_POOLS 8
+
+/* Statistics of one pcs_run_load run (latencies in microseconds, weighted by
+ * the channels each step carried). */
+typedef struct pcs_load_stats {
+    long long requests, finished, peak_concurrent, steps, blocks;
+    double wall_s, audio_s;
+    double latency_p50_us, latency_p99_us, latency_max_us;
+    double miss_rate;                 /* channel blocks whose step ended after the next release */
+    int n_pools;
+    int pool_block[PCS_LOAD_MAX_POOLS];
+    long long pool_steps[PCS_LOAD_MAX_POOLS], pool_blocks[PCS_LOAD_MAX_POOLS];
+    double pool_p50_us[PCS_LOAD_MAX_POOLS], pool_p99_us[PCS_LOAD_MAX_POOLS], pool_miss_rate[PCS_LOAD_MAX_POOLS];
+} pcs_load_stats;
+
+/*
+ * Real-time serving loop in native code (the counterpart of the reference's
+ * audio callback loop, src/pcRTMulti.cpp:138-185 and :303-365, which runs one
+ * fixed convolver and counts late callbacks).  Pools pools[0..n_pools) of
+ * base block sizes pool_block[] step every pool_block / fs seconds on a
+ * monotonic clock.  Request r arrives at arrival[r] seconds after the start,
+ * joins pool pool_of[r] with channels[r] channels (IR irs[c] for its channels
+ * c at the prefix sum of channels, ir_len[r] taps each; layout num_levels[r]
+ * levels at the prefix sum of num_levels in N_flat / P_flat) when the pool's
+ * HBM budget admits it (in arrival order), reads frames[r] samples per
+ * channel from the float32 buffer noise (a seeded offset per channel), and
+ * leaves when they are done.  Outputs are discarded.  Per step the latency
+ * from its release to its completion is recorded, and a deadline miss when
+ * it ends after the next release.  Stops after max_seconds.  Runs on the
+ * calling thread; pcs handles must not be used elsewhere meanwhile.
+ */
+int pcs_run_load(pcs_handle* const* pools, const int* pool_block, int n_pools, int n_req, const double* arrival,
+                 const int* pool_of, const int* channels, const long long* frames, const float* const* irs,
+                 const int* ir_len, const int* num_levels, const int* N_flat, const int* P_flat, const float* noise,
+                 long long noise_len, unsigned long long seed, int max_concurrent, double max_seconds, double fs,
+                 pcs_load_stats* stats);
+
 /* Size of the static device scratch array used by pc_convolve_noalloc. */
 #define PC_NOALLOC_SCRATCH_BYTES (32 << 20)
 

@@ -18,7 +18,7 @@ LIB_NAME = "libpartconv_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["step_kernels.cu", "cluster_fire.cu", "engine.cu", "filter.cu", "mimo.cu", "adjoint.cu", "serve.cu", "noalloc.cu", "io.cpp", "rtdriver.cpp"]
+SOURCES = ["step_kernels.cu", "cluster_fire.cu", "engine.cu", "filter.cu", "mimo.cu", "adjoint.cu", "serve.cu", "noalloc.cu", "io.cpp", "rtdriver.cpp", "serve_loop.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 

@@ -70,6 +70,24 @@ class PCRtStats(C.Structure):
     ]
 
 
+PCS_LOAD_MAX_POOLS = 8
+
+
+class PCSLoadStats(C.Structure):
+    _fields_ = [
+        ("requests", C.c_longlong), ("finished", C.c_longlong), ("peak_concurrent", C.c_longlong),
+        ("steps", C.c_longlong), ("blocks", C.c_longlong),
+        ("wall_s", C.c_double), ("audio_s", C.c_double),
+        ("latency_p50_us", C.c_double), ("latency_p99_us", C.c_double), ("latency_max_us", C.c_double),
+        ("miss_rate", C.c_double),
+        ("n_pools", C.c_int),
+        ("pool_block", C.c_int * PCS_LOAD_MAX_POOLS),
+        ("pool_steps", C.c_longlong * PCS_LOAD_MAX_POOLS), ("pool_blocks", C.c_longlong * PCS_LOAD_MAX_POOLS),
+        ("pool_p50_us", C.c_double * PCS_LOAD_MAX_POOLS), ("pool_p99_us", C.c_double * PCS_LOAD_MAX_POOLS),
+        ("pool_miss_rate", C.c_double * PCS_LOAD_MAX_POOLS),
+    ]
+
+
 # name -> (restype, argtypes); mirrors include/partconv_gb300.h
 SIGNATURES = {
     "pc_check_layout": (C.c_int, [C.c_int, _i32p, _i32p, C.c_int, C.c_int, _i32p, C.c_char_p, C.c_int]),
@@ -140,6 +158,10 @@ SIGNATURES = {
     "pcs_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "pcs_last_error": (C.c_char_p, [C.c_void_p]),
     "pcs_destroy": (None, [C.c_void_p]),
+    "pcs_run_load": (C.c_int, [C.POINTER(C.c_void_p), _i32p, C.c_int, C.c_int, C.POINTER(C.c_double), _i32p, _i32p,
+                               C.POINTER(C.c_longlong), C.POINTER(_f32p), _i32p, _i32p, _i32p, _i32p, _f32p,
+                               C.c_longlong, C.c_ulonglong, C.c_int, C.c_double, C.c_double,
+                               C.POINTER(PCSLoadStats)]),
 }
 
 _lock = threading.Lock()

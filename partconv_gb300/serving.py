@@ -274,139 +274,62 @@ class Server:
         outputs = {r.rid: r.y for r in finished} if keep_outputs else None
         return stats, outputs
 
-    def run_load(self, requests, irs, noise: np.ndarray, max_concurrent: int = 1000, max_seconds: float = 120.0):
-        """Real-time load run for throughput and latency: like ``run`` but
-        every channel reads its input from ``noise`` (a shared float32 buffer,
-        channel c of request r starting at a seeded offset), outputs are
-        discarded, and per-tick gathers are vectorised so the host keeps up
-        with thousands of channels.  irs[r] holds request r's IRs."""
-        order = sorted(range(len(requests)), key=lambda i: requests[i]["arrival"])
-        rng = np.random.default_rng(4321)
-        pend = list(order)
-        queue = []
-        pools = self.pools
-        period = {b: b / self.fs for b in pools}
-        st = {b: dict(pid=np.zeros(0, np.int64), off=np.zeros(0, np.int64), pos=np.zeros(0, np.int64),
-                      left=np.zeros(0, np.int64), req=np.zeros(0, np.int64)) for b in pools}
-        pcs_of = {}
-        waiting = []   # (request, block size, channel ids) admitted, not yet live
-        pool_lat = {b: [] for b in pools}   # per-step latency by base block size
-        pool_blocks = {b: 0 for b in pools}
-        pool_miss = {b: 0 for b in pools}
-        next_tick = {b: 0.0 for b in pools}
-        inflight = {b: None for b in pools}
-        lat_us, lat_w, miss_w, blocks = [], [], 0, 0
-        concurrent = peak = finished = 0
-        audio = 0.0
-        nz = len(noise)
-        t0 = time.perf_counter()
-        while finished < len(requests):
-            t = time.perf_counter() - t0
-            if t > max_seconds:
-                break
-            while pend and requests[pend[0]]["arrival"] <= t:
-                queue.append(pend.pop(0))
-            while queue and concurrent < max_concurrent:
-                ri = queue[0]
-                spec = requests[ri]
-                b = spec["N0"]
-                N, P = serving_layout(spec["ir_len"], b)
-                got = []
-                ok = True
-                for ch in range(spec["channels"]):
-                    try:   # asynchronous: the spectra build while the pools keep stepping
-                        got.append(pools[b].admit(irs[ri][ch], N, P, wait=False))
-                    except PartConvError as e:
-                        if e.code not in (nat.PC_ERR_NOMEM, nat.PC_ERR_LIMIT):
-                            raise
-                        ok = False
-                        break
-                if not ok:
-                    for pid in got:
-                        pools[b].release(pid)
-                    break
-                queue.pop(0)
-                waiting.append((ri, b, got))
-                pcs_of[ri] = got
-                concurrent += 1
-                peak = max(peak, concurrent)
-            # admitted channels whose spectra are ready join at the next tick
-            if waiting:
-                for pool in pools.values():
-                    pool.poll()
-            still = []
-            for ri, b, got in waiting:
-                if not all(pools[b].is_live(pid) for pid in got):
-                    still.append((ri, b, got))
-                    continue
-                spec = requests[ri]
-                s = st[b]
-                k = len(got)
-                s["pid"] = np.concatenate([s["pid"], np.array(got, np.int64)])
-                s["off"] = np.concatenate([s["off"], rng.integers(0, nz - spec["frames"], k)])
-                s["pos"] = np.concatenate([s["pos"], np.zeros(k, np.int64)])
-                s["left"] = np.concatenate([s["left"], np.full(k, spec["frames"] // b, np.int64)])
-                s["req"] = np.concatenate([s["req"], np.full(k, ri, np.int64)])
-            waiting = still
-            progressed = False
-            for b, pool in pools.items():
-                s = st[b]
-                if inflight[b] is not None and pool.done():
-                    tick_t, nmem = inflight[b]
-                    lat = (time.perf_counter() - t0 - tick_t) * 1e6
-                    lat_us.append(lat)
-                    lat_w.append(nmem)
-                    pool_lat[b].append(lat)
-                    pool_blocks[b] += nmem
-                    if lat > period[b] * 1e6:
-                        miss_w += nmem
-                        pool_miss[b] += nmem
-                    blocks += nmem
-                    inflight[b] = None
-                    progressed = True
-                    # channels whose last block just completed leave the pool
-                    done = s["left"] == 0
-                    if done.any():
-                        for ri in np.unique(s["req"][done]):
-                            for pid in pcs_of.pop(int(ri)):
-                                pool.release(pid)
-                            finished += 1
-                            concurrent -= 1
-                            audio += requests[int(ri)]["channels"] * requests[int(ri)]["frames"] / self.fs
-                        keep = ~done
-                        for key in s:
-                            s[key] = s[key][keep]
-                if inflight[b] is None and len(s["pid"]) and next_tick[b] <= t:
-                    idx = s["off"] + s["pos"] * b
-                    self._in[b].numpy()[s["pid"]] = noise[idx[:, None] + np.arange(b)]
-                    s["pos"] += 1
-                    s["left"] -= 1
-                    tick_t = time.perf_counter() - t0
-                    if next_tick[b] < tick_t - period[b]:
-                        next_tick[b] = tick_t
-                    next_tick[b] += period[b]
-                    pool.step(self._in[b].data_ptr(), self._out[b].data_ptr(), int(s["pid"].max()) + 1)
-                    inflight[b] = (tick_t, len(s["pid"]))
-                    progressed = True
-            if not progressed:
-                time.sleep(20e-6)
-        wall = time.perf_counter() - t0
-        lat = np.array(lat_us)
-        w = np.array(lat_w, np.float64)
-        order_l = np.argsort(lat)
-        cw = np.cumsum(w[order_l]) / max(w.sum(), 1.0)
-        pct = lambda q: float(lat[order_l][min(np.searchsorted(cw, q), len(lat) - 1)]) if len(lat) else None  # noqa: E731
-        return {"requests": len(requests), "finished": finished, "peak_concurrent": peak, "wall_s": wall,
-                "audio_s": audio, "audio_s_per_s": audio / wall if wall > 0 else 0.0, "blocks": blocks,
-                "latency_us_p50": pct(0.50), "latency_us_p99": pct(0.99),
-                "latency_us_max": float(lat.max()) if len(lat) else None,
-                "deadline_miss_rate": miss_w / max(blocks, 1),
-                "per_block_size": {str(b): {"period_us": period[b] * 1e6, "steps": len(pool_lat[b]),
-                                            "blocks": pool_blocks[b],
-                                            "step_latency_us_p50": float(np.percentile(pool_lat[b], 50))
-                                            if pool_lat[b] else None,
-                                            "step_latency_us_p99": float(np.percentile(pool_lat[b], 99))
-                                            if pool_lat[b] else None,
-                                            "deadline_miss_rate": pool_miss[b] / max(pool_blocks[b], 1)}
-                                   for b in pools},
-                "launches": sum(p.kernel_launches() for p in pools.values())}
+    def run_load(self, requests, irs, noise: np.ndarray, max_concurrent: int = 1000, max_seconds: float = 120.0,
+                 seed: int = 4321):
+        """Real-time load run for throughput and latency, in native code
+        (pcs_run_load: admission, per-tick gathers, steps and latency
+        accounting run on this thread without the Python interpreter): every
+        channel reads its input from ``noise`` (a shared float32 buffer,
+        channel c of request r starting at a seeded offset) and outputs are
+        discarded.  irs[r] holds request r's IRs (one per channel)."""
+        blocks = sorted(self.pools)
+        idx = {b: i for i, b in enumerate(blocks)}
+        n = len(requests)
+        keep = []   # arrays the native loop reads
+        arrival = np.array([r["arrival"] for r in requests], np.float64)
+        pool_of = np.array([idx[r["N0"]] for r in requests], np.int32)
+        chans = np.array([r["channels"] for r in requests], np.int32)
+        frames = np.array([r["frames"] for r in requests], np.int64)
+        ir_len = np.array([r["ir_len"] for r in requests], np.int32)
+        M, Nf, Pf, ptrs = [], [], [], []
+        for ri, r in enumerate(requests):
+            N, P = serving_layout(r["ir_len"], r["N0"])
+            M.append(len(N))
+            Nf += list(N)
+            Pf += list(P)
+            for ch in range(r["channels"]):
+                a = np.ascontiguousarray(irs[ri][ch], np.float32)
+                assert len(a) == r["ir_len"]
+                keep.append(a)
+                ptrs.append(a.ctypes.data_as(nat._f32p))
+        M = np.array(M, np.int32)
+        Nf = np.array(Nf, np.int32)
+        Pf = np.array(Pf, np.int32)
+        noise = np.ascontiguousarray(noise, np.float32)
+        handles = (C.c_void_p * len(blocks))(*[self.pools[b]._h for b in blocks])
+        pblock = np.array(blocks, np.int32)
+        ip = lambda a: a.ctypes.data_as(nat._i32p)  # noqa: E731
+        st = nat.PCSLoadStats()
+        lib = nat.lib()
+        rc = lib.pcs_run_load(handles, ip(pblock), len(blocks), n, arrival.ctypes.data_as(C.POINTER(C.c_double)),
+                              ip(pool_of), ip(chans), frames.ctypes.data_as(C.POINTER(C.c_longlong)),
+                              (nat._f32p * max(1, len(ptrs)))(*ptrs), ip(ir_len), ip(M), ip(Nf), ip(Pf),
+                              noise.ctypes.data_as(nat._f32p), len(noise), int(seed), int(max_concurrent),
+                              float(max_seconds), float(self.fs), C.byref(st))
+        if rc != nat.PC_OK:
+            raise PartConvError(rc, "pcs_run_load failed: " + "; ".join(
+                self.pools[b]._lib.pcs_last_error(self.pools[b]._h).decode() for b in blocks))
+        return {"requests": int(st.requests), "finished": int(st.finished), "peak_concurrent": int(st.peak_concurrent),
+                "wall_s": st.wall_s, "audio_s": st.audio_s,
+                "audio_s_per_s": st.audio_s / st.wall_s if st.wall_s > 0 else 0.0, "blocks": int(st.blocks),
+                "steps": int(st.steps),
+                "latency_us_p50": st.latency_p50_us, "latency_us_p99": st.latency_p99_us,
+                "latency_us_max": st.latency_max_us, "deadline_miss_rate": st.miss_rate,
+                "per_block_size": {str(blocks[i]): {"period_us": blocks[i] / self.fs * 1e6,
+                                                    "steps": int(st.pool_steps[i]), "blocks": int(st.pool_blocks[i]),
+                                                    "step_latency_us_p50": st.pool_p50_us[i],
+                                                    "step_latency_us_p99": st.pool_p99_us[i],
+                                                    "deadline_miss_rate": st.pool_miss_rate[i]}
+                                   for i in range(len(blocks))},
+                "launches": sum(p.kernel_launches() for p in self.pools.values()),
+                "loop": "native (pcs_run_load)"}

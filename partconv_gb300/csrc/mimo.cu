@@ -23,8 +23,12 @@
 //   K3 output IFFTs   -- inverse FFT of Yf_o, output ring (levels >= 1) or
 //                        the step's output: level 0 plus the due slices of
 //                        the other levels, in level order.
-// H is stored [output][input][part][bin] and streamed once per block: the
-// MAC is bound by HBM bandwidth.
+// H is streamed once per block: the MAC is bound by HBM bandwidth.  It is
+// stored tile-major, [output][bin tile][input][part][bins of the tile], with
+// each level's bins cut into fixed tiles (the bin slices the MAC tasks take),
+// so one MAC task streams one contiguous range of H (about 40 KB: its inputs'
+// rows of the tile, parts adjacent, in the order it sums them) instead of a
+// 0.4 KB segment of every (input, part) row.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,7 +56,9 @@ constexpr int kMaxMacTerms = 2048;  // (input, part) terms one MAC task sums
 
 struct MLevel {
     int N, logN, P, T, s_blocks, cs, rmask, npart;
-    float2* H;      // [nO][nI][P][cs]
+    int ntile;           // bin tiles of a row
+    const int* tstart;   // [ntile + 1]: first bin of each tile (the last entry is cs)
+    float2* H;      // [nO][tile][nI][P][tile width]
     float2* X;      // [nI][P][cs]
     float2* Yp;     // [nO][npart][2][cs]
     float2* Yf;     // [nO][cs]
@@ -181,6 +187,17 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 
 // ---------------------------------------------------------------------------
 // K2: MAC tasks (fire sums and spread partial sums)
+//
+// Measured and rejected on the 64 x 64 workload (us per launch; this kernel
+// with the tile-major H: 31.0, with the row-major H before it: 32.5):
+//   * H streamed into shared memory by cp.async stages (4 x 8 KB per CTA, no
+//     registers held by the copies): 67 -- the input-spectrum loads became a
+//     chain of round trips per stage, behind two barriers each;
+//   * four outputs per task, one input-spectrum load feeding four filter
+//     loads (twice the filter bytes in flight per thread, a quarter of the
+//     CTAs): 32.4;
+//   * terms in part-major order (consecutive inputs of one part; input
+//     spectra then far apart): 35.1.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {
@@ -223,13 +240,14 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
         int sl = slot_bt - p;
         if (sl < 0) sl += P;
         xoff[j] = ((i * P + sl) * cs) >> 1;
-        hoff[j] = ((i * P + p) * cs) >> 1;
+        hoff[j] = ((i * P + p) * (t.k1 - t.k0)) >> 1;
     }
     __syncthreads();
     // the tables depend only on the task and the step: built before the
     // wait for the input spectra of this step
     cudaGridDependencySynchronize();
-    const float4* H4 = reinterpret_cast<const float4*>(l.H + (size_t)o * nI * P * cs + k);
+    // this task's tile of H: [input][part][width] at o nI P cs + k0 nI P
+    const float4* H4 = reinterpret_cast<const float4*>(l.H + (size_t)o * nI * P * cs + (size_t)t.k0 * nI * P + (k - t.k0));
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
@@ -322,6 +340,7 @@ __global__ void __launch_bounds__(NT) mimo_yifft_kernel(const MBank* __restrict_
 template <int NT, int MAXB>
 __global__ void __launch_bounds__(NT) mimo_spectra_kernel(const float* __restrict__ irs, int ir_len, int nI, int nO,
                                                           int N, int logN, int P, int cs, long long start, float2* H,
+                                                          const int* __restrict__ tstart, int ntile,
                                                           const float2* W, int wlog) {
     extern __shared__ float4 dyn_smem[];
     float2* s = reinterpret_cast<float2*>(dyn_smem);
@@ -344,13 +363,25 @@ __global__ void __launch_bounds__(NT) mimo_spectra_kernel(const float* __restric
     const Twiddles tw{twt, logN};
     fft_smem<NT, MAXB>(s, N, logN, tw, false);
     const float inv = 1.0f / (float)(2 * N);
-    float2* dst = H + (size_t)row * cs;
+    // bin k of path (i, o), part p goes to its tile: H[o][tile][i][p][k - tile start]
+    float2* Ho = H + (size_t)o * nI * P * cs;
+    const int ip = i * P + p;
+    auto put = [&](int kb, float2 v) {
+        int lo = 0, hi = ntile;   // tile t with tstart[t] <= kb < tstart[t + 1]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (tstart[mid] <= kb) lo = mid;
+            else hi = mid;
+        }
+        const int k0 = tstart[lo], w = tstart[lo + 1] - k0;
+        Ho[(size_t)k0 * nI * P + (size_t)ip * w + (kb - k0)] = v;
+    };
     for (int k = threadIdx.x; k <= N / 2; k += NT) {
         const int nk = (k == 0) ? 0 : N - k;
         float2 xk, xnk;
         rfft_split(s[k], s[nk], k, logN, tw, xk, xnk);
-        dst[k] = make_float2(xk.x * inv, xk.y * inv);
-        if (N - k != k) dst[N - k] = make_float2(xnk.x * inv, xnk.y * inv);
+        put(k, make_float2(xk.x * inv, xk.y * inv));
+        if (N - k != k) put(N - k, make_float2(xnk.x * inv, xnk.y * inv));
     }
 }
 
@@ -388,6 +419,7 @@ struct pcm_handle {
     MTask* d_tasks = nullptr;
     std::vector<int> off[3], cnt[3];
     std::vector<double> mac_bytes;   // algorithmic bytes of K2 per phase
+    std::vector<std::vector<int>> tiles;   // per level: bin tile starts (last entry cs)
     size_t state_bytes_total = 0;
     std::vector<std::pair<void*, size_t>> state;   // zeroed by reset
     long long frame_num = 0;
@@ -564,6 +596,36 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
         if ((long)((n_in + l.npart - 1) / l.npart) * std::max(l.P - p_lo, 0) > kMaxMacTerms ||
             (long)n_in * 2 > kMaxMacTerms || (long)n_in * l.P * l.cs >= (1L << 31))
             return mfail(h, PC_ERR_LIMIT, "MIMO layout too large for one MAC task (inputs x parts)");
+        // the level's fixed bin tiles: the slices its MAC tasks take (level 0:
+        // the whole row; larger levels: each phase's slice of bins), cut into
+        // tiles of at most kMacBins bins
+        {
+            std::vector<int> ts;
+            auto tiles_of = [&](int lo, int hi) {
+                const int n = hi - lo;
+                const int nt = (n + kMacBins - 1) / kMacBins;
+                const int per = ((n + nt - 1) / nt + 1) & ~1;
+                for (int k = lo; k < hi; k += per) ts.push_back(k);
+            };
+            if (l.T > 1 && l.P >= 2) {
+                const int nch = l.T - 1;
+                for (int j = 0; j < nch; ++j) {
+                    const int lo = (int)(((long)j * l.cs / nch) & ~1L);
+                    const int hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
+                    if (hi > lo) tiles_of(lo, hi);
+                }
+            } else {
+                tiles_of(0, l.cs);
+            }
+            ts.push_back(l.cs);
+            l.ntile = (int)ts.size() - 1;
+            int* d_ts = nullptr;
+            MCK(malloc_zero(h, &d_ts, ts.size(), false), "alloc tiles");
+            MCK(cudaMemcpyAsync(d_ts, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice, h->stream),
+                "upload tiles");
+            l.tstart = d_ts;
+            h->tiles.push_back(ts);
+        }
         MCK(malloc_zero(h, &l.H, (size_t)n_out * n_in * l.P * l.cs, false), "alloc H");
         MCK(malloc_zero(h, &l.X, (size_t)n_in * l.P * l.cs, true), "alloc");
         MCK(malloc_zero(h, &l.Yp, (size_t)n_out * l.npart * 2 * l.cs, true), "alloc");
@@ -574,15 +636,15 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
         switch (cls_of(l.N)) {
             case 0:
                 mimo_spectra_kernel<256, 1><<<rows, 256, smem, h->stream>>>(d_irs, ir_len, n_in, n_out, l.N, l.logN, l.P,
-                                                                            l.cs, s, l.H, W, kWlog);
+                                                                            l.cs, s, l.H, l.tstart, l.ntile, W, kWlog);
                 break;
             case 1:
                 mimo_spectra_kernel<512, 2><<<rows, 512, smem, h->stream>>>(d_irs, ir_len, n_in, n_out, l.N, l.logN, l.P,
-                                                                            l.cs, s, l.H, W, kWlog);
+                                                                            l.cs, s, l.H, l.tstart, l.ntile, W, kWlog);
                 break;
             default:
                 mimo_spectra_kernel<512, 8><<<rows, 512, smem, h->stream>>>(d_irs, ir_len, n_in, n_out, l.N, l.logN, l.P,
-                                                                            l.cs, s, l.H, W, kWlog);
+                                                                            l.cs, s, l.H, l.tstart, l.ntile, W, kWlog);
                 break;
         }
         MCK(cudaGetLastError(), "MIMO spectra");
@@ -596,12 +658,6 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
     std::vector<std::vector<MTask>> lists[3];
     for (auto& v : lists) v.assign(h->H, {});
     h->mac_bytes.assign(h->H, 0.0);
-    auto tiles = [&](int lo, int hi, std::vector<std::pair<int, int>>& out) {
-        const int n = hi - lo;
-        const int nt = (n + kMacBins - 1) / kMacBins;
-        const int per = ((n + nt - 1) / nt + 1) & ~1;
-        for (int k = lo; k < hi; k += per) out.push_back({k, std::min(hi, k + per)});
-    };
     for (int g = 0; g < h->H; ++g) {
         for (int L = 0; L < M; ++L) {
             const MLevel& l = B.lv[L];
@@ -609,10 +665,10 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
             const bool fires = (g + 1 + l.s_blocks) % l.T == 0;
             if (fires) {
                 for (int i = 0; i < n_in; ++i) lists[0][g].push_back(MTask{0, L, i, 0, 0, 0, 0, 0});
-                std::vector<std::pair<int, int>> tl;
-                tiles(0, l.cs, tl);
+                const std::vector<int>& ts = h->tiles[L];   // the level's fixed tiles
                 for (int o = 0; o < n_out; ++o)
-                    for (auto& kk : tl) lists[1][g].push_back(MTask{1, L, o, kk.first, kk.second, 0, n_in, 0});
+                    for (size_t t = 0; t + 1 < ts.size(); ++t)
+                        lists[1][g].push_back(MTask{1, L, o, ts[t], ts[t + 1], 0, n_in, 0});
                 for (int o = 0; o < n_out; ++o) lists[2][g].push_back(MTask{3, L, o, 0, 0, 0, 0, 0});
                 const int np = (l.T == 1 && l.P >= 2) ? 2 : 1;
                 // H rows of parts 0 (and 1) of every path, X rows once per input
@@ -635,8 +691,10 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
                 hi = (j == nch - 1) ? l.cs : (int)(((long)(j + 1) * l.cs / nch) & ~1L);
             }
             if (hi <= lo) continue;
-            std::vector<std::pair<int, int>> tl;
-            tiles(lo, hi, tl);
+            std::vector<std::pair<int, int>> tl;   // the level's fixed tiles within [lo, hi)
+            const std::vector<int>& ts = h->tiles[L];
+            for (size_t t = 0; t + 1 < ts.size(); ++t)
+                if (ts[t] >= lo && ts[t + 1] <= hi) tl.push_back({ts[t], ts[t + 1]});
             for (int o = 0; o < n_out; ++o)
                 for (auto& kk : tl)
                     for (int q = 0; q < l.npart; ++q) {

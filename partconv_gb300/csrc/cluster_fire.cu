@@ -45,55 +45,6 @@ constexpr int kNT = 512;                    // threads per CTA
 constexpr int kMaxM = kClusterMaxN / kC;    // points per CTA
 constexpr int kMaxB = kMaxM / 4 / kNT;      // radix-4 butterflies per thread and stage
 constexpr int kMaxPairs = (kMaxM / 2 + 1 + kNT - 1) / kNT;   // split pairs per thread
-constexpr float kSqrtHalf = 0.70710678118654752440f;
-
-__device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }   // a * (-i)
-__device__ __forceinline__ float2 mul_pi(float2 a) { return make_float2(-a.y, a.x); }   // a * (+i)
-
-// 8-point DFT in registers, decimation in frequency (unnormalised; inverse =
-// conjugate rotations).  Output in natural order.
-__device__ __forceinline__ void dft8(float2 v[8], bool inv) {
-    // stage 1: pairs (i, i + 4), rotation w8^i of the differences
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const float2 a = cadd(v[i], v[i + 4]);
-        float2 d = csub(v[i], v[i + 4]);
-        if (i == 1) d = inv ? make_float2(kSqrtHalf * (d.x - d.y), kSqrtHalf * (d.x + d.y))
-                            : make_float2(kSqrtHalf * (d.x + d.y), kSqrtHalf * (d.y - d.x));
-        if (i == 2) d = inv ? mul_pi(d) : mul_mi(d);
-        if (i == 3) d = inv ? make_float2(-kSqrtHalf * (d.x + d.y), kSqrtHalf * (d.x - d.y))
-                            : make_float2(kSqrtHalf * (d.y - d.x), -kSqrtHalf * (d.x + d.y));
-        v[i] = a;
-        v[i + 4] = d;
-    }
-    // stage 2: in each half, pairs (i, i + 2), rotation w4^i
-#pragma unroll
-    for (int h = 0; h < 8; h += 4) {
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const float2 a = cadd(v[h + i], v[h + i + 2]);
-            float2 d = csub(v[h + i], v[h + i + 2]);
-            if (i == 1) d = inv ? mul_pi(d) : mul_mi(d);
-            v[h + i] = a;
-            v[h + i + 2] = d;
-        }
-    }
-    // stage 3: pairs (i, i + 1)
-#pragma unroll
-    for (int i = 0; i < 8; i += 2) {
-        const float2 a = cadd(v[i], v[i + 1]);
-        const float2 d = csub(v[i], v[i + 1]);
-        v[i] = a;
-        v[i + 1] = d;
-    }
-    // bit-reversed -> natural: swap 1<->4, 3<->6
-    float2 t = v[1];
-    v[1] = v[4];
-    v[4] = t;
-    t = v[3];
-    v[3] = v[6];
-    v[6] = t;
-}
 
 struct Geo {
     int n, logn, m, logm, rank;

@@ -436,4 +436,55 @@ __device__ __forceinline__ void irfft_merge(float2 yk, float2 ynk, int k, int lo
     znk = make_float2(A.x - wcB.y, -A.y + wcB.x);                 // conj(A) + i w^k conj(B)
 }
 
+// 8-point DFT in registers (used by the cluster transforms and the warp
+// transform of the level-0 inverse)
+constexpr float kSqrtHalf8 = 0.70710678118654752440f;
+__device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }   // a * (-i)
+__device__ __forceinline__ float2 mul_pi(float2 a) { return make_float2(-a.y, a.x); }   // a * (+i)
+
+// 8-point DFT in registers, decimation in frequency (unnormalised; inverse =
+// conjugate rotations).  Output in natural order.
+__device__ __forceinline__ void dft8(float2 v[8], bool inv) {
+    // stage 1: pairs (i, i + 4), rotation w8^i of the differences
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float2 a = cadd(v[i], v[i + 4]);
+        float2 d = csub(v[i], v[i + 4]);
+        if (i == 1) d = inv ? make_float2(kSqrtHalf8 * (d.x - d.y), kSqrtHalf8 * (d.x + d.y))
+                            : make_float2(kSqrtHalf8 * (d.x + d.y), kSqrtHalf8 * (d.y - d.x));
+        if (i == 2) d = inv ? mul_pi(d) : mul_mi(d);
+        if (i == 3) d = inv ? make_float2(-kSqrtHalf8 * (d.x + d.y), kSqrtHalf8 * (d.x - d.y))
+                            : make_float2(kSqrtHalf8 * (d.y - d.x), -kSqrtHalf8 * (d.x + d.y));
+        v[i] = a;
+        v[i + 4] = d;
+    }
+    // stage 2: in each half, pairs (i, i + 2), rotation w4^i
+#pragma unroll
+    for (int h = 0; h < 8; h += 4) {
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const float2 a = cadd(v[h + i], v[h + i + 2]);
+            float2 d = csub(v[h + i], v[h + i + 2]);
+            if (i == 1) d = inv ? mul_pi(d) : mul_mi(d);
+            v[h + i] = a;
+            v[h + i + 2] = d;
+        }
+    }
+    // stage 3: pairs (i, i + 1)
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        const float2 a = cadd(v[i], v[i + 1]);
+        const float2 d = csub(v[i], v[i + 1]);
+        v[i] = a;
+        v[i + 1] = d;
+    }
+    // bit-reversed -> natural: swap 1<->4, 3<->6
+    float2 t = v[1];
+    v[1] = v[4];
+    v[4] = t;
+    t = v[3];
+    v[3] = v[6];
+    v[6] = t;
+}
+
 }  // namespace pcg

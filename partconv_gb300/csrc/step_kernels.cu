@@ -487,6 +487,29 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         }
     };
 
+    // several PCs feed this output: the last one to arrive sums them in PC
+    // order (deterministic, no atomics on samples, no waiting)
+    auto mix_last = [&](float* out, long long osamp, long long och) {
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            const int o = tk.out_ch;
+            const int cnt = bank.out_off[o + 1] - bank.out_off[o];
+            *s_last = (atomicAdd(&bank.mix_cnt[o], 1) == cnt - 1);
+        }
+        __syncthreads();
+        if (!*s_last) return;
+        __threadfence();
+        const int o = tk.out_ch;
+        const int j0 = bank.out_off[o], j1 = bank.out_off[o + 1];
+        for (int i = tid; i < N0; i += NT) {
+            float v = 0.0f;
+            for (int j = j0; j < j1; ++j) v += __ldcg(&bank.pcs[bank.out_pcs[j]].pcout[i]);
+            out[i * osamp + (long long)o * och] = v;
+        }
+        if (tid == 0) bank.mix_cnt[o] = 0;
+    };
+
     if (early) forward_pass();
 
     // earlier steps' kernels have completed and their writes are visible
@@ -649,28 +672,7 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
         else if (tk.mix_mode == 2) tk.pcout[i] = v;
         for (int z = 0; z < tk.zero_outs; ++z) out[i * osamp + (long long)bank.zero_list[tk.zero_off + z] * och] = 0.0f;
     }
-    if (tk.mix_mode != 2) return;
-
-    // several PCs feed this output: the last one to arrive sums them in PC
-    // order (deterministic, no atomics on samples, no waiting)
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-        const int o = tk.out_ch;
-        const int cnt = bank.out_off[o + 1] - bank.out_off[o];
-        *s_last = (atomicAdd(&bank.mix_cnt[o], 1) == cnt - 1);
-    }
-    __syncthreads();
-    if (!*s_last) return;
-    __threadfence();
-    const int o = tk.out_ch;
-    const int j0 = bank.out_off[o], j1 = bank.out_off[o + 1];
-    for (int i = tid; i < N0; i += NT) {
-        float v = 0.0f;
-        for (int j = j0; j < j1; ++j) v += __ldcg(&bank.pcs[bank.out_pcs[j]].pcout[i]);
-        out[i * osamp + (long long)o * och] = v;
-    }
-    if (tid == 0) bank.mix_cnt[o] = 0;
+    if (tk.mix_mode == 2) mix_last(out, osamp, och);
 }
 
 // 16-byte global -> shared copies that bypass the registers (L2-cached)

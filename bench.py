@@ -16,8 +16,12 @@ per-stream drop-in path (one handle and one pc_run call per stream per
 block) is timed on a bounded sample as ``plain_gpu``.  ``cpu_baseline`` is
 the oracle restatement of the reference CPU path on all host cores.
 
---impl reference times that CPU restatement alone (the reference's FFTW
-build cannot be compiled here) on a bounded sample per step.
+--impl reference times that CPU restatement alone on a bounded sample per
+step.  The reference's own PartConvFilter code (built against an FFTW
+stand-in as the oracle's pin) uses SSE3 intrinsics and compiles on x86_64
+hosts only; on other hosts the restatement (bit for bit the reference's
+code on the strict schedule; timed here on the minimum-latency schedule,
+the same transforms and MACs per block) stands in.
 """
 from __future__ import annotations
 
@@ -253,7 +257,7 @@ def run_reference(args):
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": workload_name(S, args.samples, frames, N0), "sample": sample},
         "cpu_baseline": {"value": v, "unit": "audio-s/s", "cores": threads, "kind": "port",
-                         "sample": sample + "; restated CPU path (own FFT); reference FFTW build unavailable"},
+                         "sample": sample + "; CPU restatement of the reference path on the minimum-latency schedule (the same transforms and MACs per block as the reference's own code, which the restatement matches bit for bit on its strict schedule; that code needs SSE3, x86_64 only)"},
         "e2e": {"value": v, "unit": "audio-s/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -461,7 +465,7 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, sample, _ = cpu_baseline(c, x_host, frames)
         cpu = {"value": v, "unit": "audio-s/s", "cores": cores, "kind": "port",
-               "sample": sample + "; restated CPU path (own FFT); reference FFTW build unavailable"}
+               "sample": sample + "; CPU restatement of the reference path on the minimum-latency schedule (the same transforms and MACs per block as the reference's own code, which the restatement matches bit for bit on its strict schedule; that code needs SSE3, x86_64 only)"}
 
     if rank == 0:
         bps = bytes_per_sample(c["layouts"])

@@ -42,9 +42,9 @@ extern "C" {
 #define PC_PLANAR 1
 
 /* Largest block size a level may use (the FFT length is twice this).  The
- * pc_* engine transforms blocks above 16384 with a cluster of CTAs; the
- * MIMO (pcm_*), differentiable (pcd_*), serving (pcs_*) and PartConvFilter
- * (pcf_*) paths take blocks up to 16384 and return PC_ERR_LIMIT above. */
+ * pc_* engine and PartConvFilter (pcf_*) transform blocks above 16384 with a
+ * cluster of CTAs; the MIMO (pcm_*), differentiable (pcd_*) and serving
+ * (pcs_*) paths take blocks up to 16384 and return PC_ERR_LIMIT above. */
 #define PC_MAX_BLOCK 65536
 /* Most levels one convolver may have. */
 #define PC_MAX_LEVELS 16

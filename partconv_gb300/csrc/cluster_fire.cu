@@ -332,14 +332,109 @@ __global__ void __cluster_dims__(kC, 1, 1) __launch_bounds__(kNT)
     cl.sync();   // no CTA leaves while others may still read its shared memory
 }
 
+// PartConvFilter::runLevel (src/partconv.cpp:354-490) for one level with
+// 16384 < N <= 65536, one cluster: window = [win_old | blk] (the previous and
+// this call's delay block), forward transform into ring slot bcurr mod P,
+// Y = sum_p X[(bcurr - p) mod P] H[p] with p ascending, inverse transform,
+// the first N samples to out.  win_old then holds blk.  H and the ring use
+// the cluster bin order.
+__global__ void __cluster_dims__(kC, 1, 1) __launch_bounds__(kNT)
+    cluster_filter_level_kernel(int N, int P, int cs, unsigned bcurr, const float2* __restrict__ H, float2* X,
+                                float* win_old, const float* blk, float* out, const float2* W, int wlog) {
+    extern __shared__ float4 dyn_smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int tid = threadIdx.x;
+    float2* S = reinterpret_cast<float2*>(dyn_smem);
+    float2* twt = S + kMaxM;
+    Geo g;
+    setup_geo(g, N, W, wlog, twt);
+    float2* rem[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) rem[r] = cl.map_shared_rank(S, r);
+    // complex point j = rank m + j2 <- window samples 2j, 2j + 1; CTAs of
+    // rank < kC / 2 read win_old, the others blk
+    const int w0 = 2 * g.rank * g.m;
+    for (int j2 = tid; j2 < g.m; j2 += kNT) {
+        const int t = w0 + 2 * j2;
+        S[sidx<true>(j2)] = t < N ? *reinterpret_cast<const float2*>(win_old + t)
+                                  : *reinterpret_cast<const float2*>(blk + (t - N));
+    }
+    __syncthreads();
+    // each CTA overwrites only the part of win_old it has read
+    if (w0 < N)
+        for (int i = tid; i < 2 * g.m; i += kNT) win_old[w0 + i] = blk[w0 + i];
+    cl.sync();
+    column_pass_fwd(g, rem, cl);
+    const Twiddles tw{twt, g.logm};
+    fft_smem<kNT, kMaxB, true>(S, g.m, g.logm, tw, false);
+    cl.sync();
+
+    const unsigned uP = (unsigned)P;
+    float2* Xs = X + (size_t)(bcurr % uP) * cs;
+    auto mac = [&](int pos, float2 x) {
+        float2 y = cmul(x, __ldg(&H[pos]));
+        for (int p = 1; p < P; ++p) {
+            const unsigned sl = (bcurr - (unsigned)p + uP) % uP;
+            y = cadd(y, cmul(__ldcg(&X[(size_t)sl * cs + pos]), __ldg(&H[(size_t)p * cs + pos])));
+        }
+        return y;
+    };
+    const int np = pair_count(g);
+    float2 zo[kMaxPairs][2];
+#pragma unroll
+    for (int i = 0; i < kMaxPairs; ++i) {
+        const int pi = tid + i * kNT;
+        if (pi >= np) continue;
+        const Pair pq = pair_at(g, pi);
+        const float2 zk = S[sidx<true>(pq.k2)];
+        const bool self = (pq.nk == pq.k);
+        const float2 znk = (pq.k == 0 || self) ? zk : rem[pq.pr][sidx<true>(pq.pk2)];
+        float2 xk, xnk;
+        split_pair(g, zk, znk, pq.k, xk, xnk);
+        const int pk = bin_pos(g, pq.k), pnk = bin_pos(g, pq.nk);
+        Xs[pk] = xk;
+        if (!self) Xs[pnk] = xnk;
+        const float2 yk = mac(pk, xk);
+        const float2 ynk = self ? yk : mac(pnk, xnk);
+        merge_pair(g, yk, ynk, pq.k, zo[i][0], zo[i][1]);
+    }
+    cl.sync();   // every CTA has read the forward spectra
+#pragma unroll
+    for (int i = 0; i < kMaxPairs; ++i) {
+        const int pi = tid + i * kNT;
+        if (pi >= np) continue;
+        const Pair pq = pair_at(g, pi);
+        S[sidx<true>(pq.k2)] = zo[i][0];
+        if (pq.k != 0 && pq.nk != pq.k) rem[pq.pr][sidx<true>(pq.pk2)] = zo[i][1];
+    }
+    cl.sync();
+    fft_smem<kNT, kMaxB, true>(S, g.m, g.logm, tw, true);
+    cl.sync();
+    column_pass_inv(g, rem, cl);
+    // complex points [0, n/2) are the block's first N samples
+    if (g.rank < kC / 2)
+        for (int j2 = tid; j2 < g.m; j2 += kNT) *reinterpret_cast<float2*>(out + w0 + 2 * j2) = S[sidx<true>(j2)];
+}
+
 size_t cluster_smem_bytes() { return sizeof(float2) * (size_t)kMaxM + sizeof(float2) * (size_t)(kMaxM / 2); }
 
 cudaError_t prepare_cluster_kernels() {
     cudaError_t e = cudaFuncSetAttribute(cluster_fire_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)cluster_smem_bytes());
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(cluster_filter_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cluster_smem_bytes());
+    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(cluster_spectra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)cluster_smem_bytes());
+}
+
+cudaError_t launch_cluster_filter_level(int N, int P, int cs, unsigned bcurr, const float2* H, float2* X,
+                                        float* win_old, const float* blk, float* out, const float2* W, int wlog,
+                                        cudaStream_t st) {
+    cluster_filter_level_kernel<<<kC, kNT, cluster_smem_bytes(), st>>>(N, P, cs, bcurr, H, X, win_old, blk, out, W,
+                                                                       wlog);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_cluster_fire(int ntasks, const Bank& bank, const Task* tasks, const RunState& rs,

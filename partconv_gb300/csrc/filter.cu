@@ -29,7 +29,7 @@ using namespace pcg;
 
 namespace {
 
-constexpr int kWlog = 15;
+constexpr int kWlog = 17;   // twiddle table: real transforms of blocks up to 65536
 
 // One level block of the reference schedule.  win_old: the previous delay
 // block (first half of the window, updated in place); blk: this call's delay
@@ -200,7 +200,7 @@ cudaError_t dalloc(pcf_handle* h, T** p, size_t n) {
     return e;
 }
 
-int cls_of(int N) { return N <= 1024 ? 0 : (N <= 4096 ? 1 : 2); }
+int cls_of(int N) { return N <= 1024 ? 0 : (N <= 4096 ? 1 : (N <= kMaxBlockOneCta ? 2 : 3)); }
 
 cudaError_t launch_level(pcf_handle* h, int L) {
     const int N = h->N[L], logN = (int)std::lround(std::log2((double)N)), P = h->P[L], cs = N + 2;
@@ -209,6 +209,15 @@ cudaError_t launch_level(pcf_handle* h, int L) {
     float* out = h->ybuf[1 - h->rd[L]][L];
     const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
+        case 3:   // a cluster of CTAs (cluster_fire.cu); H and X in the cluster bin order
+            h->launches += 1;
+            {
+                cudaError_t e = launch_cluster_filter_level(N, P, cs, h->bcurr[L], h->H[L], h->X[L], h->win_old[L],
+                                                            blk, out, h->W, kWlog, h->stream);
+                if (e == cudaSuccess && L == 0)
+                    e = cudaMemcpyAsync(h->out0, out, sizeof(float) * N, cudaMemcpyDeviceToDevice, h->stream);
+                return e;
+            }
         case 0:
             filter_level_kernel<256, 1><<<1, 256, smem, h->stream>>>(N, logN, P, cs, h->bcurr[L], h->H[L], h->X[L],
                                                                      h->win_old[L], blk, out, h->W, kWlog);
@@ -256,8 +265,6 @@ int pcf_setup(pcf_handle* h, int M, const int* N, int* P, const float* ir, int i
     char msg[256];
     int r = pc_check_layout(M, Nv.data(), Pv.data(), (int)hv.size(), relaxed_check, delays.data(), msg, sizeof msg);
     if (r) return ffail(h, r, msg);
-    if (Nv[M - 1] > kMaxBlockOneCta)
-        return ffail(h, PC_ERR_LIMIT, "PartConvFilter levels are limited to blocks of 16384 (larger blocks: pc_* engine)");
     for (int i = 0; i < M; ++i) P[i] = Pv[i];
     if (Nv[0] < 16) return ffail(h, PC_ERR_LIMIT, "block size of level 0 must be >= 16");
     FCK(cudaGetDevice(&h->device), "cudaGetDevice");
@@ -298,6 +305,7 @@ int pcf_setup(pcf_handle* h, int M, const int* N, int* P, const float* ir, int i
     h->H.resize(M);
     h->X.resize(M);
     h->win_old.resize(M);
+    std::vector<SpectraJob> big;   // filter rows of cluster levels, one job per part
     long start = 0;
     for (int L = 0; L < M; ++L) {
         const int n = Nv[L], cs = n + 2, logN = (int)std::lround(std::log2((double)n));
@@ -322,6 +330,15 @@ int pcf_setup(pcf_handle* h, int M, const int* N, int* P, const float* ir, int i
         FCK(dalloc(h, &d.d_mem, (size_t)d.bufferSize * d.frameSize), "alloc");
         const size_t smem = (size_t)12 * n;
         switch (cls_of(n)) {
+            case 3:
+                for (int p = 0; p < Pv[L]; ++p) {
+                    const long row = start + (long)p * n;
+                    const long left = (long)hv.size() - row;
+                    big.push_back(SpectraJob{d_ir + std::min<long>(row, (long)hv.size()),
+                                             (int)std::max<long>(0, std::min<long>(left, n)), n, logN,
+                                             h->H[L] + (size_t)p * cs});
+                }
+                break;
             case 0:
                 filter_spectra_kernel<256, 1><<<Pv[L], 256, smem, h->stream>>>(d_ir, (long long)hv.size(), start, n, logN,
                                                                                cs, h->H[L], h->W, kWlog);
@@ -336,8 +353,17 @@ int pcf_setup(pcf_handle* h, int M, const int* N, int* P, const float* ir, int i
                 break;
         }
         FCK(cudaGetLastError(), "filter spectra");
-        h->launches += 1;
+        if (cls_of(n) < 3) h->launches += 1;
         start += (long)n * Pv[L];
+    }
+    if (!big.empty()) {
+        SpectraJob* d_jobs = nullptr;
+        FCK(dalloc(h, &d_jobs, big.size()), "alloc");
+        FCK(cudaMemcpyAsync(d_jobs, big.data(), sizeof(SpectraJob) * big.size(), cudaMemcpyHostToDevice, h->stream),
+            "upload");
+        FCK(launch_cluster_spectra((int)big.size(), d_jobs, h->W, kWlog, h->stream), "filter spectra");
+        h->launches += 1;
+        FCK(cudaStreamSynchronize(h->stream), "spectra sync");   // before the job table goes out of scope
     }
     FCK(dalloc(h, &h->out0, Nv[0]), "alloc");
     FCK(dalloc(h, &h->d_y, Nv[0]), "alloc");

@@ -1,4 +1,4 @@
-// kernels.h -- launchers for the kernels in step_kernels.cu.
+// kernels.h -- launchers for the kernels in step_kernels.cu and cluster_fire.cu.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -27,7 +27,6 @@ constexpr int kClusterCtas = 8;          // CTAs per class-3 fire
 constexpr int kClusterMaxN = 65536;      // largest block of class 3
 // threads per CTA of a class
 int class_threads(int cls);
-// bins one spread task covers
 // default bins and parts per spread task (the tile shape pc_set_tiles overrides)
 int spread_task_bins();
 int spread_task_parts();
@@ -69,6 +68,10 @@ cudaError_t prepare_cluster_kernels();
 cudaError_t launch_cluster_fire(int ntasks, const Bank& bank, const Task* tasks, const RunState& rs,
                                 const RunState* rs_dev, int step_in_batch, cudaStream_t st, bool pdl, int prio);
 cudaError_t launch_cluster_spectra(int njobs, const SpectraJob* jobs, const float2* W, int wlog, cudaStream_t st);
+// PartConvFilter's runLevel for such a level (filter.cu), one cluster
+cudaError_t launch_cluster_filter_level(int N, int P, int cs, unsigned bcurr, const float2* H, float2* X,
+                                        float* win_old, const float* blk, float* out, const float2* W, int wlog,
+                                        cudaStream_t st);
 
 }  // namespace pcg
 

@@ -144,3 +144,68 @@ def test_large_top_level_with_four_blocks_per_step(gpu):
     pcs[0]["P"] = list(m.layout(0)[1])
     ref = oracle.OracleMulti(256, 1, 1, pcs).run(x)
     assert _rel(y[:, 0], ref[:, 0]) <= TOL
+
+
+@pytest.mark.parametrize("N,P,L", [([1024, 4096, 16384, 32768], [6, 6, 2, 0], 130000),
+                                   ([4096, 16384, 65536], [6, 6, 0], 254000)])
+def test_filter_large_levels_match_oracle(gpu, N, P, L):
+    """PartConvFilter (the fine-grained API tune.py drives) with levels of
+    32768 and 65536 samples: the reference's sync_levels -> input ->
+    runLevel -> output sequence (src/partconvMulti.cpp:849-909), strict and
+    relaxed, against the oracle's PartConvFilter and an FP64 convolution."""
+    from partconv_gb300 import partconv
+
+    rng = np.random.default_rng(L)
+    h = wl.decaying_ir(rng, L, 1.0)
+    f = partconv.PartConvFilter()
+    assert f.setup(len(N), N, P, h) == 0, f.last_error
+    o = oracle.OracleFilter(N, P, h)
+    assert list(f.num_parts) == list(o.num_parts)
+    N0 = N[0]
+    x = np.zeros(N0 * (L // N0 + 2 * N[-1] // N0 + 4), np.float32)
+    x[:L // 2] = (0.1 * rng.standard_normal(L // 2)).astype(np.float32)
+    for relaxed in (0, 1):
+        f.reset()
+        o.reset()
+        ys, rs = [], []
+        for b in range(len(x) // N0):
+            blk = x[b * N0:(b + 1) * N0]
+            if relaxed:
+                f.sync_levels_relaxed()
+                o.sync_levels_relaxed()
+                ys.append(f.output_relaxed())
+                rs.append(o.output_relaxed())
+            else:
+                f.sync_levels()
+                o.sync_levels()
+            f.input(blk)
+            o.input(blk)
+            for lv in range(len(N)):
+                if b % (N[lv] // N0) == 0:
+                    f.runLevel(lv)
+                    o.runLevel(lv)
+            if not relaxed:
+                ys.append(f.output())
+                rs.append(o.output())
+        y, r = np.concatenate(ys), np.concatenate(rs)
+        err = wl.rel_l2(y, r)
+        print(f"{N} relaxed={relaxed}: rel L2 vs oracle {err:.2e}")
+        assert err <= TOL
+        if not relaxed:
+            assert wl.rel_l2(y, wl.conv_fp64(x, h, len(x))) <= TOL
+    assert f.cleanup() == 0
+
+
+def test_filter_bench_large_level(gpu):
+    """tune.py's bench() on a layout whose top level is 65536 samples."""
+    from partconv_gb300 import partconv
+
+    f = partconv.PartConvFilter()
+    N, P = partconv.intArray(3), partconv.intArray(3)
+    for i, (n, p) in enumerate([(4096, 6), (16384, 6), (65536, 2)]):
+        N[i], P[i] = n, p
+    assert f.setup(3, N, P, None, 2, "wisdom.wis") == 0
+    for lv in range(3):
+        t = f.bench(lv, 20, 3, 0.1)
+        assert 0 < t < 0.1
+    assert f.cleanup() == 0

@@ -48,9 +48,8 @@ using namespace pcg;
 namespace {
 
 constexpr int kWlog = 15;
-constexpr int kMacNT = 128;        // MAC CTA: 4 groups x 32 lanes, two bins per lane
-constexpr int kMacLanes = 32;
-constexpr int kMacBins = 2 * kMacLanes;
+constexpr int kMacNT = 128;        // MAC CTA: threads = (bin-pair column, term group) pairs
+constexpr int kMacMaxBins = 128;   // widest bin tile (64 columns of two bins: two term groups)
 constexpr int kMaxMimoLevels = 8;
 constexpr int kMaxMacTerms = 2048;  // (input, part) terms one MAC task sums
 
@@ -188,11 +187,17 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 // ---------------------------------------------------------------------------
 // K2: MAC tasks (fire sums and spread partial sums)
 //
-// Measured and rejected on the 64 x 64 workload (us per launch; this kernel
-// with the tile-major H: 31.0, with the row-major H before it: 32.5):
+// Measured on the 64 x 64 workload (us per launch): this kernel 30.7; with
+// at most four term groups of 32 columns (a third of the threads idle on
+// 44-bin tiles) 31.0; with the row-major H before the tile-major one 32.5.
+// Rejected:
 //   * H streamed into shared memory by cp.async stages (4 x 8 KB per CTA, no
 //     registers held by the copies): 67 -- the input-spectrum loads became a
 //     chain of round trips per stage, behind two barriers each;
+//   * a task's whole H tile copied into shared memory by cp.async before the
+//     grid dependency wait, input spectra through registers one batch ahead:
+//     46.6-48.6 -- 46 KB per CTA leaves four CTAs per SM, and each CTA's
+//     input-spectrum round trips start only once its tile has landed;
 //   * four outputs per task, one input-spectrum load feeding four filter
 //     loads (twice the filter bytes in flight per thread, a quarter of the
 //     CTAs): 32.4;
@@ -201,15 +206,19 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {
-    __shared__ float4 red[(kMacNT / kMacLanes - 1) * kMacLanes];
+    __shared__ float4 red[kMacNT];
     cudaTriggerProgrammaticLaunchCompletion();
-    constexpr int G = kMacNT / kMacLanes;
     const MBank& bank = *bank_p;
     const MTask t = tasks[blockIdx.x];
     const MLevel& l = bank.lv[t.level];
-    const int lane = threadIdx.x % kMacLanes, g = threadIdx.x / kMacLanes;
+    // ncol bin-pair columns (a float4 each) x G term groups; consecutive
+    // threads walk a row of the tile, then the next term's row, which
+    // follows it in memory
+    const int ncol = (t.k1 - t.k0) >> 1;
+    const int G = kMacNT / ncol;
+    const int lane = threadIdx.x % ncol, g = threadIdx.x / ncol;
     const int k = t.k0 + 2 * lane;
-    const bool active = k < t.k1;
+    const bool active = g < G;
     const int o = t.ch, P = l.P, cs = l.cs, nI = bank.nI;
     const long long c = rs.step_base;
 
@@ -269,11 +278,10 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
                 if (j0 + u * G < J) acc = f4mac(acc, xv[u], hv[u]);
         }
     }
-    if (g > 0) red[(g - 1) * kMacLanes + lane] = acc;
+    if (g > 0 && active) red[(g - 1) * ncol + lane] = acc;
     __syncthreads();
-    if (g != 0 || !active) return;
-#pragma unroll
-    for (int j = 1; j < G; ++j) acc = f4add(acc, red[(j - 1) * kMacLanes + lane]);
+    if (g != 0) return;
+    for (int j = 1; j < G; ++j) acc = f4add(acc, red[(j - 1) * ncol + lane]);
     if (t.kind == 1) {
         const bool has_spread = (l.T == 1) ? P >= 3 : P >= 2;
         if (has_spread) {
@@ -598,13 +606,31 @@ int pcm_setup(pcm_handle* h, int fs, int buffer_size, int n_in, int n_out, int M
             return mfail(h, PC_ERR_LIMIT, "MIMO layout too large for one MAC task (inputs x parts)");
         // the level's fixed bin tiles: the slices its MAC tasks take (level 0:
         // the whole row; larger levels: each phase's slice of bins), cut into
-        // tiles of at most kMacBins bins
+        // tiles of at most kMacMaxBins bins
         {
             std::vector<int> ts;
+            // a MAC CTA runs floor(kMacNT / columns) term groups over a tile's
+            // columns: pick the tile count that keeps most threads busy (a
+            // small charge per extra tile for its CTA's fixed work)
             auto tiles_of = [&](int lo, int hi) {
                 const int n = hi - lo;
-                const int nt = (n + kMacBins - 1) / kMacBins;
-                const int per = ((n + nt - 1) / nt + 1) & ~1;
+                int best_nt = 0;
+                double best = -1.0;
+                for (int nt = (n + kMacMaxBins - 1) / kMacMaxBins; nt <= 16; ++nt) {
+                    const int per = ((n + nt - 1) / nt + 1) & ~1;
+                    if (per < 2 || (nt - 1) * per >= n) continue;
+                    double busy = 0.0;
+                    for (int k = lo; k < hi; k += per) {
+                        const int nc = (std::min(per, hi - k)) >> 1;
+                        busy += (double)((kMacNT / nc) * nc) / kMacNT;
+                    }
+                    const double score = busy / nt - 0.05 * nt;
+                    if (score > best) {
+                        best = score;
+                        best_nt = nt;
+                    }
+                }
+                const int per = ((n + best_nt - 1) / best_nt + 1) & ~1;
                 for (int k = lo; k < hi; k += per) ts.push_back(k);
             };
             if (l.T > 1 && l.P >= 2) {

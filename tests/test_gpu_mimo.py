@@ -32,8 +32,7 @@ def _oracle_mimo(irs, x, N, P, threads=None):
     ([64, 256, 1024], [4, 3, 0], 3, 4, 5000),
     ([128, 2048], [16, 15], 2, 3, 1 << 15),
     ([256], [0], 4, 1, 3000),
-    # 398 older parts per spread task: too many filter rows to stage in
-    # shared memory, so the MAC streams them through registers instead
+    # 398 older parts per spread task (one input each): long MAC term lists
     ([64], [400], 8, 2, 25600),
 ])
 def test_mimo_matches_oracle(gpu, N, P, n_in, n_out, L):

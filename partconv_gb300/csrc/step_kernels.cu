@@ -460,31 +460,33 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             h0s[bnk != k ? bnk : N + 1] = pnk;
         }
     };
-    auto merge_pass = [&]() {     // Y = X_b H_0 + (X_{b-1} H_1 + Yp), inverse merge into s
-        __syncthreads();
-        for (int k = tid; k <= half; k += NT) {
+    // Y = X_b H_0 + (X_{b-1} H_1 + Yp[b & 1]) and the inverse merge into s, by
+    // bin pair (k, N - k) -- the pairs the forward split gave this thread, so
+    // it reads only its own h0s entries; H_1 waits in yacc since the prologue.
+    // xp, yp: this thread's X_{b-1} and partial sums of its pairs.
+    auto merge_pass = [&](const float2 (*xp)[2], const float2 (*yp)[2]) {
+#pragma unroll
+        for (int j = 0; j < kXr; ++j) {
+            const int k = tid + j * NT;
+            if (k > half) continue;
             const int bnk = N - k;
-            const float2 yk = cadd(h0s[k], yacc[k]);
-            const float2 ynk = cadd(h0s[bnk != k ? bnk : N + 1], yacc[bnk]);
+            float2 ak = make_float2(0.f, 0.f), ank = ak;
+            if (use_x1) {
+                ak = cmul(xp[j][0], yacc[k]);
+                ank = cmul(xp[j][1], yacc[bnk]);
+            }
+            if (use_yp) {
+                ak = cadd(ak, yp[j][0]);
+                ank = cadd(ank, yp[j][1]);
+            }
+            const float2 yk = cadd(h0s[k], ak);
+            const float2 ynk = cadd(h0s[bnk != k ? bnk : N + 1], ank);
             float2 zk, znk;
             irfft_merge(yk, ynk, k, logN, tw, zk, znk);
             s[k] = zk;
             if (k != 0 && k != half) s[N - k] = znk;
         }
         __syncthreads();
-    };
-    // yacc (holding H_1) <- X_{b-1} H_1 + Yp[b & 1], same float4 mapping as the prefetch
-    auto partial_pass = [&](const float4* xa, const float4* ya) {
-#pragma unroll
-        for (int i = 0; i < C::MAXK; ++i) {
-            const int kk = 2 * (tid + i * NT);
-            if (kk < 2 * npair) {
-                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (use_x1) acc = f4mul(xa[i], *reinterpret_cast<const float4*>(yacc + kk));
-                if (use_yp) acc = f4add(acc, ya[i]);
-                *reinterpret_cast<float4*>(yacc + kk) = acc;
-            }
-        }
     };
 
     // several PCs feed this output: the last one to arrive sums them in PC
@@ -525,7 +527,8 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
     if constexpr (C::PREFETCH) {
         // ---- dependent inputs: input-ring history (unless EARLY), previous
         //      spectrum, partial sums, the other levels' due output slices ----
-        float4 wo[C::MAXQ], xa[C::MAXK], ya[C::MAXK];
+        float4 wo[C::MAXQ];
+        float2 xp[kXr][2], yp[kXr][2];
         if (!early) {
 #pragma unroll
             for (int i = 0; i < C::MAXQ; ++i) {
@@ -537,14 +540,21 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
             }
         }
 #pragma unroll
-        for (int i = 0; i < C::MAXK; ++i) {
-            const int kk = 2 * (tid + i * NT);
-            if (kk < 2 * npair) {
-                if (use_x1) xa[i] = __ldcg(reinterpret_cast<const float4*>(X1 + kk));
+        for (int j = 0; j < kXr; ++j) {
+            const int k = tid + j * NT;
+            if (k <= half) {
+                const int bnk = N - k;
+                if (use_x1) {
+                    xp[j][0] = __ldcg(&X1[k]);
+                    xp[j][1] = __ldcg(&X1[bnk]);
+                }
                 if (use_yp) {
-                    ya[i] = __ldcg(reinterpret_cast<const float4*>(Ypb + kk));
-                    for (int q = 1; q < npart; ++q)
-                        ya[i] = f4add(ya[i], __ldcg(reinterpret_cast<const float4*>(Ypb + q * rstride + kk)));
+                    yp[j][0] = __ldcg(&Ypb[k]);
+                    yp[j][1] = __ldcg(&Ypb[bnk]);
+                    for (int q = 1; q < npart; ++q) {
+                        yp[j][0] = cadd(yp[j][0], __ldcg(&Ypb[q * rstride + k]));
+                        yp[j][1] = cadd(yp[j][1], __ldcg(&Ypb[q * rstride + bnk]));
+                    }
                 }
             }
         }
@@ -562,9 +572,8 @@ __device__ __forceinline__ void fire_body(const Bank& bank, const Task& tk, cons
                 *reinterpret_cast<float4*>(tk.xring + (ta & tk.rin_mask)) = wv[i];
             }
         }
-        partial_pass(xa, ya);
         if (!early) forward_pass();
-        merge_pass();
+        merge_pass(xp, yp);
     } else {
         // ---- dependent inputs (no prefetch): input-ring history ----------------
         {
@@ -1022,7 +1031,7 @@ __device__ __forceinline__ void fire_multi(const Bank& bank, const Task& tk, con
 // LANES: threads per spread part-group (bins per spread task / 2), the tile
 // width of the handle, one instance per width.
 template <class C, bool MULTI = false, int LANES = 64>
-__global__ void __launch_bounds__(C::NT) step_kernel(Bank bank, const Task* __restrict__ tasks, RunState rs_val,
+__global__ void __launch_bounds__(C::NT, C::PREFETCH ? 3 : 1) step_kernel(Bank bank, const Task* __restrict__ tasks, RunState rs_val,
                                                      const RunState* rs_dev, int step_in_batch) {
     extern __shared__ float4 dyn_smem[];
     __shared__ __align__(16) Task tk;

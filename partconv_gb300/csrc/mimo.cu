@@ -202,7 +202,9 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 //     loads (twice the filter bytes in flight per thread, a quarter of the
 //     CTAs): 32.4;
 //   * terms in part-major order (consecutive inputs of one part; input
-//     spectra then far apart): 35.1.
+//     spectra then far apart): 35.1;
+//   * the filter loads as ld.global.nc.L1::no_allocate with a 128- or
+//     256-byte L2 prefetch size instead of __ldcs: 30.49 against 30.51.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {

@@ -151,6 +151,7 @@ struct pc_handle {
 
     std::vector<DevPC> h_pcs;
     std::vector<DevLevel> h_lv;
+    std::vector<int> lv_cls;   // kernel class of each level's fires (spectra layout follows it)
     Bank bank{};
     int H = 1;        // hyperperiod (base steps)
     int G = 64;       // base steps per captured graph (multiple of H and KB)
@@ -555,6 +556,26 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             }
         }
     }
+    // Kernel class per level.  A fire within its step sits on the step chain,
+    // where its latency counts: levels of 8192 and 16384 samples then run on
+    // a cluster (class 3) when few of them share a handle, so that all their
+    // clusters fit the GPU at once; otherwise (and for deferred fires, which
+    // overlap later steps) one CTA per fire.
+    h->lv_cls.assign(nlv, 0);
+    {
+        int li = 0, instep_big = 0;
+        for (auto& p : h->specs)
+            for (size_t L = 0; L < p.N.size(); ++L, ++li)
+                if (L > 0 && KB == 1 && dfl[li] == 0 && p.N[L] >= kClusterInStepMinN && p.N[L] <= kMaxBlockOneCta)
+                    ++instep_big;
+        const bool few = instep_big * kClusterCtas <= kClusterInStepMaxCtas;
+        li = 0;
+        for (auto& p : h->specs)
+            for (size_t L = 0; L < p.N.size(); ++L, ++li) {
+                h->lv_cls[li] = fire_class_of(p.N[L]);
+                if (few && L > 0 && KB == 1 && dfl[li] == 0 && p.N[L] >= kClusterInStepMinN) h->lv_cls[li] = 3;
+            }
+    }
 
     // ---- descriptors (host) ----------------------------------------------------------
     h->h_pcs.assign(npc, DevPC{});
@@ -635,7 +656,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             t.rin_mask = d.rin_mask;
             t.lv_index = li;
             t.scale = d.scale;
-            const int cls = fire_class_of(l.N);
+            const int cls = h->lv_cls[li];
             // bytes a fire must move: H0 row read, new X row written, the
             // partial-sum row read (level 0 and deferred levels also X_{b-1}
             // and H_1 rows), the 2N-sample window read, N samples written;
@@ -741,7 +762,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
             const DevLevel& l = h->h_lv[li];
             const DevPC& d = h->h_pcs[l.pc];
             const double C = l.N + 1.0;
-            const int cls = fire_class_of(l.N);
+            const int cls = h->lv_cls[li];
             if (l.T == 1) {   // level 0: KB blocks, parts < 2 KB in the fire
                 Task t = fire_task(li);
                 const int Q = std::min(l.P, QC);
@@ -929,9 +950,9 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                            h->stream),
            "upload tasks");
     for (int cls = 0; cls < kClasses; ++cls) h->class_maxN[cls] = 0;
-    for (auto& l : h->h_lv) {
-        const int cls = fire_class_of(l.N);
-        h->class_maxN[cls] = std::max(h->class_maxN[cls], l.N);
+    for (int li = 0; li < nlv; ++li) {
+        const int cls = h->lv_cls[li];
+        h->class_maxN[cls] = std::max(h->class_maxN[cls], h->h_lv[li].N);
     }
     // the level-0 class also runs spread tasks; its smem must fit its fires
     if (h->class_maxN[h->l0_class] == 0) h->class_maxN[h->l0_class] = N0;
@@ -1014,7 +1035,7 @@ int do_setup(pc_handle* h, int fs, int buffer_size, int n_in, int n_out, std::ve
                     jb.N = l.N;
                     jb.logN = l.logN;
                     jb.dst = l.H + (size_t)q * l.cs;
-                    jobs[fire_class_of(l.N)].push_back(jb);
+                    jobs[h->lv_cls[h->h_pcs[i].lv0 + L]].push_back(jb);
                 }
                 s += (long)l.N * l.P;
             }

@@ -25,6 +25,8 @@ constexpr int kNumClasses = 4;
 constexpr int kMaxBlockOneCta = 16384;   // largest block one CTA transforms (classes 0-2)
 constexpr int kClusterCtas = 8;          // CTAs per class-3 fire
 constexpr int kClusterMaxN = 65536;      // largest block of class 3
+constexpr int kClusterInStepMinN = 8192;    // smallest in-step level that may run on a cluster
+constexpr int kClusterInStepMaxCtas = 64;   // ... when its handle's in-step cluster fires need at most this many CTAs
 // threads per CTA of a class
 int class_threads(int cls);
 // default bins and parts per spread task (the tile shape pc_set_tiles overrides)

@@ -209,3 +209,39 @@ def test_filter_bench_large_level(gpu):
         t = f.bench(lv, 20, 3, 0.1)
         assert 0 < t < 0.1
     assert f.cleanup() == 0
+
+
+@pytest.mark.parametrize("streams", [1, 3, 9])
+def test_in_step_large_levels_on_clusters_or_ctas(gpu, streams):
+    """Minimum-slack layouts whose 8192- and 16384-sample levels fire within
+    their step: with at most eight such fires per handle they run on 8-CTA
+    clusters, with more on one CTA each.  Both match the oracle; pc_run
+    block by block and pc_process give the same bits."""
+    rng = np.random.default_rng(40 + streams)
+    N0 = 256
+    layouts = [([256, 2048, 16384], [8, 7, 1]), ([256, 1024, 8192], [4, 7, 1])]
+    pcs = []
+    for i in range(streams):
+        N, P = layouts[i % 2]
+        L = sum(n * p for n, p in zip(N[:-1], P[:-1])) + int(rng.integers(N[-1], 3 * N[-1]))
+        pcs.append(dict(ir=wl.decaying_ir(rng, L, 0.5), N=N, P=P, in_ch=i, out_ch=i))
+    L = max(len(p["ir"]) for p in pcs)
+    frames = -(-(L + 8 * N0) // N0) * N0
+    x = np.zeros((frames, streams), np.float32)
+    x[:16 * N0] = (0.1 * rng.standard_normal((16 * N0, streams))).astype(np.float32)
+    m = PartConvMulti()
+    m.setup_layout(48000, N0, streams, streams, pcs)
+    pcs = [p | dict(P=list(m.layout(i)[1])) for i, p in enumerate(pcs)]
+    y = m.process(x)
+    ref = oracle.OracleMulti(N0, streams, streams, pcs).run(x)
+    for o in range(streams):
+        err = _rel(y[:, o], ref[:, o])
+        print(f"{streams} streams, output {o}: rel L2 vs oracle {err:.2e}")
+        assert err <= TOL
+    m.reset()
+    yb = np.zeros_like(y)
+    out = np.zeros(N0 * streams, np.float32)
+    for b in range(frames // N0):
+        m.run(out, np.ascontiguousarray(x[b * N0:(b + 1) * N0]), N0)
+        yb[b * N0:(b + 1) * N0] = out.reshape(N0, streams)
+    assert np.array_equal(yb, y)

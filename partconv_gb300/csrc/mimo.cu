@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 //   * terms in part-major order (consecutive inputs of one part; input
 //     spectra then far apart): 35.1;
 //   * the filter loads as ld.global.nc.L1::no_allocate with a 128- or
-//     256-byte L2 prefetch size instead of __ldcs: 30.49 against 30.51.
+//     256-byte L2 prefetch size instead of __ldcs: 30.49 against 30.51;
+//   * 256-thread CTAs (four per SM): 31.4; 64-thread CTAs: 47.8.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {

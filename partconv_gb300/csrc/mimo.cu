@@ -91,6 +91,26 @@ __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
+// L2 eviction policy for a MAC task's filter rows: the level-0 rows (read
+// every base step) are kept in L2 ahead of the larger levels' rows, which
+// stream through once per level block
+__device__ __forceinline__ unsigned long long l2_policy(bool keep) {
+    unsigned long long p;
+    if (keep)
+        asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    else
+        asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+// 16-byte read-only load with an L2 cache policy, not kept in L1
+__device__ __forceinline__ float4 ld_policy(const float4* ptr, unsigned long long pol) {
+    float4 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(ptr), "l"(pol));
+    return v;
+}
+
 __device__ __forceinline__ long long block_of(const MLevel& l, long long c) {   // newest block fired by step c
     return (c + 1 + l.s_blocks) / l.T - 1;
 }
@@ -206,6 +226,10 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 //   * the filter loads as ld.global.nc.L1::no_allocate with a 128- or
 //     256-byte L2 prefetch size instead of __ldcs: 30.49 against 30.51;
 //   * 256-thread CTAs (four per SM): 31.4; 64-thread CTAs: 47.8.
+// Kept: the level-0 filter rows (68 MB, read every base step) loaded with an
+// L2 evict-last policy and the larger levels' rows with evict-first, so the
+// level-0 rows stay in L2 between steps: 30.5 -> 28.5 (evict-normal for
+// level 0: 28.8).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {
@@ -261,6 +285,7 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
     // this task's tile of H: [input][part][width] at o nI P cs + k0 nI P
     const float4* H4 = reinterpret_cast<const float4*>(l.H + (size_t)o * nI * P * cs + (size_t)t.k0 * nI * P + (k - t.k0));
     const float4* X4 = reinterpret_cast<const float4*>(l.X + k);
+    const unsigned long long hpol = l2_policy(t.level == 0);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
         // eight 128-thread CTAs per SM (64 registers): more, smaller CTAs in
@@ -273,7 +298,7 @@ __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __rest
                 const int j = j0 + u * G;
                 if (j < J) {
                     xv[u] = __ldcg(X4 + xoff[j]);
-                    hv[u] = __ldcs(H4 + hoff[j]);
+                    hv[u] = ld_policy(H4 + hoff[j], hpol);
                 }
             }
 #pragma unroll

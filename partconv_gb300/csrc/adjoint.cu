@@ -70,8 +70,11 @@ struct IJob {
     int dst, mode, pad;
 };
 
+// (the 512-thread, two-butterfly instances here and in difft_kernel are held
+// to 32 registers so that four CTAs fit an SM: the 512 windows of a
+// 4096-sample level over a batch of 8 then run in one wave instead of two)
 template <int NT, int MAXB>
-__global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs, DPtrs ptr, int N, int logN,
+__global__ void __launch_bounds__(NT, NT * MAXB == 1024 ? 4 : 1) dfft_kernel(const FJob* __restrict__ jobs, DPtrs ptr, int N, int logN,
                                                   const float2* W, int wlog) {
     extern __shared__ float4 dyn_smem[];
     float2* s = reinterpret_cast<float2*>(dyn_smem);
@@ -102,7 +105,7 @@ __global__ void __launch_bounds__(NT) dfft_kernel(const FJob* __restrict__ jobs,
 }
 
 template <int NT, int MAXB>
-__global__ void __launch_bounds__(NT) difft_kernel(const IJob* __restrict__ jobs, DPtrs ptr, int N, int logN,
+__global__ void __launch_bounds__(NT, NT * MAXB == 1024 ? 4 : 1) difft_kernel(const IJob* __restrict__ jobs, DPtrs ptr, int N, int logN,
                                                    const float2* W, int wlog) {
     extern __shared__ float4 dyn_smem[];
     float2* s = reinterpret_cast<float2*>(dyn_smem);
@@ -302,7 +305,10 @@ cudaError_t launch_fft(int N, int logN, const FJob* jobs, int njobs, const DPtrs
     if (njobs <= 0) return cudaSuccess;
     const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
-        case 0: dfft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
+        case 0:   // one radix-4 butterfly per thread and stage: N / 4 threads
+            if (N <= 512) dfft_kernel<128, 1><<<njobs, 128, smem, st>>>(jobs, ptr, N, logN, W, kWlog);
+            else dfft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog);
+            break;
         case 1: dfft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
         default: dfft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
     }
@@ -314,7 +320,10 @@ cudaError_t launch_ifft(int N, int logN, const IJob* jobs, int njobs, const DPtr
     if (njobs <= 0) return cudaSuccess;
     const size_t smem = (size_t)12 * N;
     switch (cls_of(N)) {
-        case 0: difft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
+        case 0:
+            if (N <= 512) difft_kernel<128, 1><<<njobs, 128, smem, st>>>(jobs, ptr, N, logN, W, kWlog);
+            else difft_kernel<256, 1><<<njobs, 256, smem, st>>>(jobs, ptr, N, logN, W, kWlog);
+            break;
         case 1: difft_kernel<512, 2><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
         default: difft_kernel<512, 8><<<njobs, 512, smem, st>>>(jobs, ptr, N, logN, W, kWlog); break;
     }

@@ -226,6 +226,10 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 //   * the filter loads as ld.global.nc.L1::no_allocate with a 128- or
 //     256-byte L2 prefetch size instead of __ldcs: 30.49 against 30.51;
 //   * 256-thread CTAs (four per SM): 31.4; 64-thread CTAs: 47.8.
+//   * the larger levels' tasks first in the launch (level 0's last): 30.6;
+//   * (probes) level-0 tasks alone 16.2, level-1 tasks alone 21.4, and 21.7
+//     with the level-1 filter loads at the addresses of an interleaved
+//     [term][task][column] layout: DRAM page locality is not what limits it.
 // Kept: the level-0 filter rows (68 MB, read every base step) loaded with an
 // L2 evict-last policy and the larger levels' rows with evict-first, so the
 // level-0 rows stay in L2 between steps: 30.5 -> 28.5 (evict-normal for

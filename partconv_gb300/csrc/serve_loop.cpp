@@ -139,6 +139,21 @@ extern "C" int pcs_run_load(pcs_handle* const* pools, const int* pool_block, int
     double audio = 0.0;
     int rc = PC_OK;
 
+    // The tick loop must not wait on the host allocator: the pinned per-pool
+    // blocks are sized up front (a pool's channel ids stay below the channels
+    // of its requests).  Page-locking the impulse responses for the run, so
+    // that admissions upload them by DMA, was measured and rejected: deadline
+    // misses alike, but single stalls of 65-124 ms.
+    {
+        std::vector<long long> need(n_pools, 0);
+        for (int i = 0; i < n_req; ++i) need[pool_of[i]] += channels[i];
+        for (int b = 0; b < n_pools; ++b)
+            if (need[b] > 0 && !ensure(b, (int)std::min<long long>(need[b], 1 << 16))) {
+                free_all();
+                return PC_ERR_NOMEM;
+            }
+    }
+
     const auto t0 = Clock::now();
     auto now = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
     while (finished < n_req && rc == PC_OK) {

@@ -227,6 +227,8 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 //     256-byte L2 prefetch size instead of __ldcs: 30.49 against 30.51;
 //   * 256-thread CTAs (four per SM): 31.4; 64-thread CTAs: 47.8.
 //   * the larger levels' tasks first in the launch (level 0's last): 30.6;
+//   * input spectra through L1 (__ldg): 28.2 against 28.5, not worth relying
+//     on the read-only path for data the previous kernel wrote;
 //   * (probes) level-0 tasks alone 16.2, level-1 tasks alone 21.4, and 21.7
 //     with the level-1 filter loads at the addresses of an interleaved
 //     [term][task][column] layout: DRAM page locality is not what limits it.

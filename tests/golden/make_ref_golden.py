@@ -43,6 +43,10 @@ CASES = {
                             dict(N=[128], P=[0], L=2500, in_ch=1, out_ch=0, scale=0.5),
                             dict(N=[128, 1024], P=[14, 0], L=3000, in_ch=0, out_ch=1, mute=1),
                             dict(N=[128, 512], P=[6, 0], L=1800, in_ch=1, out_ch=1, scale=-1.25)], 3072),
+    # a 32768-sample top level (the fires of blocks above 16384 run on clusters
+    # of CTAs on the GPU), as the reference's own pc.config layouts use
+    "ref_large_32768": (256, 1, 1, [dict(N=[256, 2048, 32768], P=[14, 30, 0], L=110000, in_ch=0, out_ch=0)],
+                        4096),
 }
 
 

@@ -251,3 +251,20 @@ def test_top_level_partconv_module_name():
     a = top.intArray(4)
     a[2] = 7
     assert a[2] == 7 and top.doubleArray(2)[1] == 0.0
+
+
+def test_waiter_signals_across_threads():
+    """Waiter (src/partconvMulti.h:152-165): waitFor returns once another
+    thread has changed the value to the target, and times out otherwise."""
+    import threading
+
+    from partconv_gb300.multi import Waiter
+
+    w = Waiter(0)
+    assert not w.waitFor(1, timeout=0.01)
+    t = threading.Timer(0.05, w.changeAndSignal, args=(1,))
+    t.start()
+    assert w.waitFor(1, timeout=5.0)
+    t.join()
+    w.changeAndSignal(2)
+    assert w.waitFor(2, timeout=0.01) and not w.waitFor(1, timeout=0.01)

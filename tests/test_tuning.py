@@ -160,3 +160,27 @@ def test_shipped_cache_is_consistent():
         assert list(best["tiles"]) == min(tc, key=lambda r: r["us_per_step"])["tiles"]
         assert {tuple(r["tiles"]) for r in tc} == set(autotune.TILE_CANDIDATES)
     assert n_layout >= 5 and n_tiles >= 1
+
+
+def test_cached_tile_shapes(tmp_path):
+    """Tile shapes from the cache without measuring: the one stored with a
+    length class's layout, and the one measured for a whole workload handle
+    (keyed by workload name, base block and PC count); misses give None."""
+    from partconv_gb300 import autotune as at
+
+    path = tmp_path / "cache.json"
+    path.write_text(json.dumps({
+        "Some GPU|N0=256|len=131072|batch=32": {
+            "best": {"N": [256, 2048, 16384], "P": [14, 14, 7], "us_per_step": 3.2, "tiles": [128, 32]},
+            "candidates": []},
+        "Some GPU|tiles|cfg2|N0=256|pcs=32": {
+            "best": {"tiles": [128, 16], "us_per_step": 2.9},
+            "candidates": [{"tiles": [128, 16], "us_per_step": 2.9}, {"tiles": [256, 16], "us_per_step": 3.4}]},
+    }))
+    assert at.cached_tiles(100000, 256, 32, cache=str(path)) == (128, 32)
+    assert at.cached_tiles(5000, 256, 32, cache=str(path)) is None
+    pcs = [dict(N=[256], P=[1])] * 32
+    assert at.choose_tiles(pcs, 256, "cfg2", cache=str(path), measure=False) == (128, 16)
+    assert at.choose_tiles(pcs[:8], 256, "cfg2", cache=str(path), measure=False) is None
+    assert at.choose_tiles(pcs, 128, "cfg2", cache=str(path), measure=False) is None
+    assert at.choose_tiles(pcs, 256, "cfg3", cache=str(path), measure=False) is None

@@ -2,6 +2,7 @@
 shapes, value ranges and determinism (the same seed gives the same arrays),
 and the layouts they name are valid.  CPU only."""
 import numpy as np
+import pytest
 
 from partconv_gb300 import workloads as wl
 from partconv_gb300.multi import check_layout
@@ -93,3 +94,33 @@ def test_fd_grads_fp64_match_analytic_gradients():
     ref_x = [2 / M * np.dot(r[b, i:i + L][: T - i], h[: T - i].astype(np.float64)) for b, i in cx]
     assert np.allclose(gh, ref_h, rtol=1e-9, atol=0)
     assert np.allclose(gx, ref_x, rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("strict", [False, True])
+@pytest.mark.parametrize("ratio", [4, 8])
+def test_chain_layout_is_valid_and_minimal(strict, ratio):
+    """chain_layout: block sizes grow by `ratio`, every level but the last
+    holds just enough parts for the next level's offset (minimum slack, or
+    the reference's strict slack), the last covers the IR, and the layout
+    passes the matching check."""
+    from partconv_gb300.multi import check_layout
+
+    for L in (5000, 70000, 300000):
+        N, P = wl.chain_layout(L, 256, ratio=ratio, max_block=65536, strict=strict)
+        assert N[0] == 256 and all(b == a * ratio or b == 65536 for a, b in zip(N, N[1:]))
+        s = 0
+        for i in range(len(N) - 1):
+            s += N[i] * P[i]
+            need = 2 * N[i + 1] - 2 * 256 if strict else N[i + 1]
+            assert s >= need and s - N[i] < need, (L, N, P)   # just enough parts
+        assert sum(n * p for n, p in zip(N, P)) >= L
+        st, _, _, msg = check_layout(N, P, L, relaxed=not strict)
+        assert st == 0, msg
+
+
+def test_algorithmic_bytes_per_sample():
+    """sum_L (8 (N_L + 1)(2 P_L + 1) + 12 N_L) / N_L: H and X ring read, new X
+    slot written, 2N window read, N outputs written per level block."""
+    N, P = [256, 2048], [14, 15]
+    want = (8 * 257 * 29 + 12 * 256) / 256 + (8 * 2049 * 31 + 12 * 2048) / 2048
+    assert wl.algorithmic_bytes_per_sample(N, P) == pytest.approx(want, rel=1e-12)

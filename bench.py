@@ -600,9 +600,9 @@ def run_mimo(args):
         "dtype": "f32", "data": "synthetic (seeded numpy PCG64, cfg seed 1003)",
         "config": {"workload": f"cfg3: {n_in}x{n_out} paths of {L} taps, {frames} frames, layout 128x16|2048x15",
                    "device_bytes": m.device_bytes(),
-                   "l2": "256 MB buffer written between timed steps (outside the events); within a step the "
-                         "level-0 filter spectra (68 MB) are kept in L2 by an evict-last policy, the level-1 "
-                         "spectra stream from HBM"},
+                   "l2": "256 MB buffer written between timed steps (outside the events); the level-0 filter "
+                         "spectra (68 MB, read every base step) are loaded with an L2 evict-last policy, the "
+                         "level-1 spectra evict-first (the spectra, 1.07 GB, exceed L2)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "mimo_mac", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak, "peak_kind": peak_kind,

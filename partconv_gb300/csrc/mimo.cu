@@ -92,8 +92,8 @@ __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
 }
 
 // L2 eviction policy for a MAC task's filter rows: the level-0 rows (read
-// every base step) are kept in L2 ahead of the larger levels' rows, which
-// stream through once per level block
+// every base step) are evicted last, the larger levels' rows, which stream
+// through once per level block, first
 __device__ __forceinline__ unsigned long long l2_policy(bool keep) {
     unsigned long long p;
     if (keep)
@@ -233,9 +233,9 @@ __global__ void __launch_bounds__(NT) mimo_xfft_kernel(const MBank* __restrict__
 //     with the level-1 filter loads at the addresses of an interleaved
 //     [term][task][column] layout: DRAM page locality is not what limits it.
 // Kept: the level-0 filter rows (68 MB, read every base step) loaded with an
-// L2 evict-last policy and the larger levels' rows with evict-first, so the
-// level-0 rows stay in L2 between steps: 30.5 -> 28.5 (evict-normal for
-// level 0: 28.8).
+// L2 evict-last policy and the larger levels' rows with evict-first, so more
+// of the level-0 rows survive in L2 between steps: 30.5 -> 28.5 (evict-normal
+// for level 0: 28.8).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMacNT, 8) mimo_mac_kernel(const MBank* __restrict__ bank_p,
                                                           const MTask* __restrict__ tasks, RunState rs) {

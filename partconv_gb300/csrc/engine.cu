@@ -35,7 +35,7 @@ using namespace pcg;
 namespace {
 
 constexpr int kWlog = 17;          // twiddle table 2^17 entries: real FFTs up to 2 * 65536
-constexpr int kMinGraphSteps = 256;   // base steps per captured graph (a multiple of the hyperperiod)
+constexpr int kMinGraphSteps = 128;   // base steps per captured graph (a multiple of the hyperperiod)
 constexpr int kMinN0 = 16;
 constexpr int kClasses = kNumClasses;
 

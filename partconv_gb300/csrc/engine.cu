@@ -1373,7 +1373,7 @@ int pc_process(pc_handle* h, float* output, const float* input, long long frames
     // Long calls run as a pipeline of chunks: the input copy of chunk i + 1
     // and the output copy of chunk i - 1 (own streams) overlap the steps of
     // chunk i (the handle's stream); the steps of one call stay in order.
-    const long long chunk = (long long)std::max(h->G, 256) * h->N0;   // a multiple of KB N0
+    const long long chunk = (long long)std::max(h->G, 128) * h->N0;   // a multiple of KB N0
     if (!h->relaxed && frames >= 2 * chunk) {
         if (!h->cin) CK(cudaStreamCreateWithFlags(&h->cin, cudaStreamNonBlocking), "stream create");
         if (!h->cout) CK(cudaStreamCreateWithFlags(&h->cout, cudaStreamNonBlocking), "stream create");

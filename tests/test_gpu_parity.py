@@ -281,7 +281,7 @@ def test_long_process_pipeline_equals_device_path(gpu, layout):
     pcs = [dict(ir=_ir(rng, 9000), N=[64, 512, 4096], P=[14, 14, 0], in_ch=0, out_ch=0),
            dict(ir=_ir(rng, 3000), N=[64, 256], P=[6, 0], in_ch=1, out_ch=0, scale=0.5),
            dict(ir=_ir(rng, 5000), N=[64, 512], P=[10, 0], in_ch=1, out_ch=2)]
-    frames = N0 * 1500   # chunks of 256 blocks (the last one shorter)
+    frames = N0 * 1500   # chunks of 128 blocks (the last one shorter)
     x = (0.1 * rng.standard_normal((frames, 2))).astype(np.float32)
     xin = x if layout == PC_INTERLEAVED else np.ascontiguousarray(x.T)
     a = PartConvMulti()
